@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""
+Benchmark of the FDTD time-stepping hot path on GB300.
+
+Workload (default c2): the reference README's 395x345x73 grid (~10M cells), float32, as a
+seeded L3 photonic-crystal slab cavity with 8-cell CPML on all six faces, an Ey Gaussian
+point source and the Poynting vector on. One step = update_E, the soft source add,
+update_H and update_S over the whole grid (the loop of opencl_fdtd's fdtd.py:162-175).
+Inputs (~1 GB of fields) are far larger than the 129 MB L2, so no flush is needed between
+steps.
+
+Printed as one JSON line:
+  value       Mcell-updates/s with every buffer resident in HBM (device-timed, CUDA events)
+  e2e         the same metric through the public Simulation API, with the per-step source
+              sample copied host->device from pinned memory and one field sample read back
+  roofline    the dominant kernel's algorithmic bytes per launch / its mean event-timed
+              duration, against the measured HBM copy bandwidth
+  step_roofline  the whole step's algorithmic bytes (84 B/cell for E+H, +12 B/cell S,
+              +32 B per CPML face-cell) per step time
+  cpu_baseline   the reference's own kernels (oracle/_ref replay; else the C restatement)
+              timed on the host cores on a bounded number of full-grid steps
+
+--impl reference times the reference's CPU implementation of the same steps instead.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-updates/s & %HBM peak, plain vs batched+learned-ABC at stated field err"
+UNIT = "Mcell-updates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="c2")
+    ap.add_argument("--e2e-steps", type=int, default=2000)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic(workload: str):
+    """dram bytes per launch per kernel from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "traffic_%s.json" % workload)
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(N: int, face_cells: int, elem: int, poynting: bool):
+    """Per-launch compulsory bytes (each input read once, each output written once)."""
+    e = N * 12 * elem + face_cells * 4 * elem           # E r/w, H r, eps r; psi_E r/w
+    h = N * 9 * elem + face_cells * 4 * elem             # H r/w, E r; psi_H r/w
+    s = 0
+    if poynting:
+        h += N * 6 * elem                                 # oS w
+        s = N * 9 * elem                                  # oS r, S w
+    step = N * 21 * elem + face_cells * 8 * elem + (N * 3 * elem if poynting else 0)
+    return {"k_yee_e": e, "k_yee_h": h, "k_poynting": s}, step
+
+
+def cpu_sample(wl, seconds: float, nthreads: int):
+    """Time full-grid steps of the reference's CPU kernels (replay) or the C restatement."""
+    from oracle import ref_replay
+    kw = wl["kwargs"]
+    eps = numpy.concatenate([e.ravel() for e in kw["epsilon"]])
+    if wl["name"] == "c2" and ref_replay.available("c2"):
+        sim = ref_replay.ReplaySimulation("c2", eps, nthreads=nthreads)
+        kind = "reference"
+    else:
+        from oracle import port
+        import copy
+        sim = port.PortSimulation(**copy.deepcopy(kw), nthreads=nthreads)
+        kind = "port"
+    N = int(numpy.prod(wl["shape"]))
+    ind = wl["source_index"]
+
+    def step(t):
+        sim.update_E([])
+        sim.E[ind] += numpy.float32(wl["wave"](t))
+        sim.update_H([])
+        if kw.get("do_poynting", True):
+            sim.update_S([])
+
+    step(0)
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        step(n + 1)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 1000:
+            break
+    return {"value": N * n / el / 1e6, "unit": UNIT, "cores": nthreads, "kind": kind,
+            "sample": "%d full-grid steps of %s (%d cells) after 1 warm-up step, %.1f s"
+                      % (n, wl["name"], N, el)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from opencl_fdtd_gb300 import workloads
+    wl = workloads.get(args.workload)
+    nthreads = os.cpu_count() or 1
+    # one step = one full-grid canonical step; the number of steps run is capped so the
+    # whole run stays within about a minute
+    base = cpu_sample(wl, seconds=2.0, nthreads=nthreads)
+    per_step = wl["shape"][0] * wl["shape"][1] * wl["shape"][2] / (base["value"] * 1e6)
+    k = max(1, min(args.steps, int(60.0 / max(per_step, 1e-6))))
+    res = cpu_sample(wl, seconds=k * per_step, nthreads=nthreads)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": round(res["value"], 3), "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * numpy.prod(wl["shape"]) / (res["value"] * 1e6), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": wl["describe"], "grid": list(wl["shape"]),
+                   "timed_steps_run": res["sample"]},
+        "cpu_baseline": {"value": round(res["value"], 3), "unit": UNIT, "cores": nthreads,
+                         "kind": res["kind"], "sample": res["sample"]},
+        "e2e": {"value": round(res["value"], 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from opencl_fdtd_gb300 import Simulation, workloads, _lib
+
+    wl = workloads.get(args.workload)
+    kw = wl["kwargs"]
+    sim = Simulation(**kw)
+    N = int(numpy.prod(wl["shape"]))
+    fc = workloads.face_cells(wl["shape"], kw["pmls"])
+    poynting = kw.get("do_poynting", True)
+    elem = 4 if kw.get("float_type", numpy.float32) == numpy.float32 else 8
+    K, W = args.steps, args.warmup
+    ind = wl["source_index"]
+    stream = sim.queue
+    waves = numpy.array([wl["wave"](t) for t in range(W + K)], dtype=numpy.float32)
+    wave_dev = torch.from_numpy(waves).cuda()
+    lib = sim._lib
+    plan = sim._plan
+    bufp = ctypes.byref(sim._buffers())
+    st = ctypes.c_void_p(stream.cuda_stream)
+    E1 = sim.E[ind:ind + 1]
+
+    def step(t, ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        _lib.check(lib.fdtd_update_e(plan, bufp, st))
+        if ev is not None:
+            ev[1].record(stream)
+        E1.add_(wave_dev[t:t + 1])
+        if ev is not None:
+            ev[2].record(stream)
+        _lib.check(lib.fdtd_update_h(plan, bufp, st))
+        if ev is not None:
+            ev[3].record(stream)
+        if poynting:
+            _lib.check(lib.fdtd_update_s(plan, bufp, st))
+        if ev is not None:
+            ev[4].record(stream)
+
+    with torch.cuda.stream(stream):
+        for t in range(W):
+            step(t)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(K)]
+        clocks = ClockSampler(local)
+        clocks.start()
+        time.sleep(0.3)
+        torch.cuda.synchronize()
+        for t in range(K):
+            step(W + t, evs[t])
+        torch.cuda.synchronize()
+        clock = clocks.stop()
+        if world > 1:
+            torch.distributed.barrier()
+    total_ms = evs[0][0].elapsed_time(evs[-1][4])
+    ke = [evs[t][0].elapsed_time(evs[t][1]) for t in range(K)]
+    kh = [evs[t][2].elapsed_time(evs[t][3]) for t in range(K)]
+    ks = [evs[t][3].elapsed_time(evs[t][4]) for t in range(K)]
+    if world > 1:
+        tt = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    ms_per_step = total_ms / K
+    value = world * N * K / (total_ms * 1e-3) / 1e6
+
+    per_launch, step_bytes = algorithmic_bytes(N, fc, elem, poynting)
+    means = {"k_yee_e": statistics.mean(ke), "k_yee_h": statistics.mean(kh)}
+    if poynting:
+        means["k_poynting"] = statistics.mean(ks)
+    dom = max(means, key=lambda k: means[k])
+    peak, peak_kind = peak_hbm()
+    achieved = per_launch[dom] / (means[dom] * 1e-3) / 1e9
+    traffic = committed_traffic(args.workload).get(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "traffic": traffic, "algorithmic_bytes_per_launch": per_launch[dom],
+                "mean_launch_ms": round(means[dom], 5),
+                "per_kernel_ms": {k: round(v, 5) for k, v in means.items()}}
+    step_gbs = step_bytes / (ms_per_step * 1e-3) / 1e9
+    step_roof = {"achieved": round(step_gbs, 1), "peak": peak, "unit": "GB/s",
+                 "frac": round(step_gbs / peak, 4), "bytes_per_step": step_bytes,
+                 "accounting": "84 B/cell E+H, +12 B/cell S, +32 B per CPML face-cell (f32)"}
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(sim, wl, args.e2e_steps, world)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_sample(wl, args.cpu_seconds, os.cpu_count() or 1)
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+            "steps": K, "warmup": W, "ms_per_step": round(ms_per_step, 5),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded L3 cavity geometry and source)",
+            "config": {"workload": wl["describe"], "grid": list(wl["shape"]), "cells": N,
+                       "cpml_face_cells": fc, "path": "drop-in update_E/H/S (two-pass + S pass)",
+                       "l2": "inputs (~%.0f MB of fields) larger than the 129 MB L2; no flush"
+                             % (sim.E.numel() * elem * (6 if poynting else 3) / 1e6),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": roofline, "step_roofline": step_roof, "clocks": clock,
+            "e2e": e2e, "gpu_launches": (3 if poynting else 2) * K,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_e2e(sim, wl, steps: int, world: int):
+    """The public API loop of fdtd.py:162-175 with the source sample copied from pinned host
+    memory each step and the driven field component read back into pinned memory."""
+    import torch
+    ind = wl["source_index"]
+    poynting = wl["kwargs"].get("do_poynting", True)
+    host_src = torch.from_numpy(numpy.array([wl["wave"](t) for t in range(steps)],
+                                            dtype=numpy.float32)).pin_memory()
+    host_probe = torch.empty(steps, dtype=torch.float32).pin_memory()
+    dev_src = torch.empty(1, dtype=torch.float32, device=sim.device)
+    E1 = sim.E[ind:ind + 1]
+    stream = sim.queue
+
+    def one(t):
+        sim.update_E([])
+        dev_src.copy_(host_src[t:t + 1], non_blocking=True)
+        E1.add_(dev_src)
+        e = sim.update_H([])
+        if poynting:
+            sim.update_S([e])
+        host_probe[t:t + 1].copy_(E1, non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        for t in range(min(20, steps)):
+            one(t)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for t in range(steps):
+            one(t)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+    N = int(numpy.prod(wl["shape"]))
+    return {"value": round(world * N * steps / el / 1e6, 2), "unit": UNIT,
+            "h2d_bytes_per_step": 4, "d2h_bytes_per_step": 4, "steps": steps,
+            "api": "Simulation.update_E/H/S + tensor source add, stream-ordered"}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,146 @@
+/*
+ * fdtd_gb300.h — C ABI of the GB300 (sm_103a) FDTD time-stepping library.
+ *
+ * The reference (opencl_fdtd) reaches its kernels through pyopencl: Simulation.__init__
+ * renders jinja2 templates into OpenCL C (opencl_fdtd/simulation.py:198-245), wraps each in an
+ * ElementwiseKernel (simulation.py:321-326) and hands back closures update_E/H/S/F/G/J that
+ * enqueue one kernel on the context's queue. This header is the boundary that replaces that
+ * FFI: a plan takes the role of the rendered, specialised kernel set, and one entry point per
+ * closure enqueues the same update on a CUDA stream.
+ *
+ * Conventions
+ *   - Every field is a flat device array of 3*N elements, components [X | Y | Z], each in C
+ *     order (x, y, z) with z fastest (opencl_fdtd/kernels/common.cl:34-52). oS holds 6*N
+ *     elements in the plane order xy, yz, zx, xz, yx, zy (update_h.cl:142-147).
+ *   - Device buffers belong to the caller (torch tensors in the Python layer) and are passed
+ *     as raw pointers on every call. A plan owns only its small coefficient tables.
+ *   - Calls are asynchronous on the given stream (a cudaStream_t passed as void*; NULL is the
+ *     legacy default stream). One plan serves one host thread at a time, as the reference's
+ *     single queue does (simulation.py:328-338).
+ *   - Every entry point returns FDTD_OK (0) or a negative status; no exception crosses the
+ *     ABI. fdtd_last_error() returns the calling thread's last message.
+ */
+#ifndef FDTD_GB300_H
+#define FDTD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDTD_ABI_VERSION 1
+
+/* status codes */
+#define FDTD_OK 0
+#define FDTD_ERR_INVALID (-1)      /* bad shape, size, pointer or option */
+#define FDTD_ERR_UNSUPPORTED (-2)  /* dtype or option combination not built */
+#define FDTD_ERR_CUDA (-3)         /* a CUDA runtime call or launch failed */
+#define FDTD_ERR_WATCHDOG (-4)     /* a bounded device-side wait gave up */
+#define FDTD_ERR_NONFINITE (-5)    /* a field watchdog found NaN/Inf */
+
+/* storage / arithmetic types (simulation.py:360-376 maps numpy float16/32/64) */
+#define FDTD_F32 0
+#define FDTD_F64 1
+
+typedef struct FdtdPmlDesc {
+    int32_t axis;        /* 0, 1, 2 for 'x', 'y', 'z' */
+    int32_t polarity;    /* 0 = 'n' (low side), 1 = 'p' (high side) */
+    int32_t thickness;   /* T cells */
+    int32_t _pad;
+    /* Host pointers to the six coefficient tables p{0,1,2}e and p{0,1,2}h (simulation.py:
+     * 284-307), each `thickness` long, indexed by depth ir (0 = outermost cell), in the
+     * plan's dtype. The plan copies them to the device. */
+    const void *p0e, *p1e, *p2e, *p0h, *p1h, *p2h;
+} FdtdPmlDesc;
+
+typedef struct FdtdBlochDesc {
+    int32_t axis;        /* 0, 1, 2 */
+    int32_t _pad;
+    double real, imag;   /* beta = real + i*imag: field(r + L) = beta * field(r) */
+} FdtdBlochDesc;
+
+typedef struct FdtdDesc {
+    int64_t shape[3];    /* (sx, sy, sz); N = sx*sy*sz must be < 2^32 */
+    int32_t dtype;       /* FDTD_F32 or FDTD_F64 */
+    int32_t uniform;     /* 1: uniform spacing dx; 0: per-axis tables in FdtdBuffers */
+    double dt;           /* rounded to dtype, as the reference's `ftype dt` argument */
+    double dx;           /* uniform spacing; the kernels use (dtype)(1.0/dx) */
+    int32_t n_pml;       /* 0..6 faces, applied in list order */
+    int32_t n_bloch;     /* 0..3 */
+    FdtdPmlDesc pml[6];
+    FdtdBlochDesc bloch[3];
+    int32_t do_poynting; /* update_H writes oS; update_S is available */
+    int32_t do_fieldsrc; /* update_J is available */
+    int32_t has_mu;      /* H updates divide dt by mu (absent in the reference) */
+    int32_t _pad;
+} FdtdDesc;
+
+typedef struct FdtdBuffers {
+    void *E, *H;             /* 3N each */
+    void *F, *G;             /* imaginary parts with Bloch boundaries, else NULL */
+    const void *eps;         /* 3N relative permittivity; +inf marks PEC */
+    const void *mu;          /* 3N relative permeability when has_mu, else NULL */
+    void *S;                 /* 3N Poynting vector when do_poynting */
+    void *oS;                /* 6N Poynting products when do_poynting */
+    const void *Jr, *Ji;     /* 3N current-source phasor when do_fieldsrc */
+    /* CPML auxiliary fields, per face in plan order, two components (u, v) each: the two
+     * axes other than the face's, in xyz order. Layout: C order of the grid shape with the
+     * face axis replaced by T, indexed by depth ir along that axis. */
+    void *psi_e[6][2], *psi_h[6][2], *psi_f[6][2], *psi_g[6][2];
+    /* non-uniform spacing: 1/dx on the E grid (H updates read these) and on the H grid
+     * (E updates read these), lengths sx, sy, sz; NULL when uniform */
+    const void *inv_de[3], *inv_dh[3];
+} FdtdBuffers;
+
+typedef struct FdtdPlan FdtdPlan;
+
+/* Returns FDTD_ABI_VERSION. */
+int fdtd_abi_version(void);
+
+/* Last error message of the calling thread ("" if none). */
+const char *fdtd_last_error(void);
+
+/* Build a plan: validates the description and uploads the coefficient tables.
+ * Replaces Simulation.__init__'s kernel generation (simulation.py:170-271). */
+int fdtd_plan_create(const FdtdDesc *desc, FdtdPlan **out);
+int fdtd_plan_destroy(FdtdPlan *plan);
+
+/* update_E (simulation.py:254; opencl_fdtd/kernels/update_e.cl): E += dt/eps * (curl H + psi),
+ * advancing psi_e. With Bloch boundaries it reads G at the wrapped faces. */
+int fdtd_update_e(FdtdPlan *plan, const FdtdBuffers *buf, void *stream);
+/* update_H (simulation.py:255; update_h.cl): H -= dt[/mu] * (curl E - psi), advancing psi_h,
+ * and writes oS when do_poynting. With Bloch boundaries it reads F at the wrapped faces. */
+int fdtd_update_h(FdtdPlan *plan, const FdtdBuffers *buf, void *stream);
+/* update_S (simulation.py:256-257; update_s.cl): S = dt/8 * (sum of four oS terms). */
+int fdtd_update_s(FdtdPlan *plan, const FdtdBuffers *buf, void *stream);
+/* update_F / update_G (simulation.py:258-264): the imaginary halves of a Bloch pair,
+ * advancing psi_f / psi_g. */
+int fdtd_update_f(FdtdPlan *plan, const FdtdBuffers *buf, void *stream);
+int fdtd_update_g(FdtdPlan *plan, const FdtdBuffers *buf, void *stream);
+/* update_J (simulation.py:265-271; update_j.cl): E += c*Jr + s*Ji for
+ * box = {xmin, xmax, ymin, ymax, zmin, zmax} (half-open, clipped to the grid). */
+int fdtd_update_j(FdtdPlan *plan, const FdtdBuffers *buf, void *stream, double c, double s,
+                  const int64_t box[6]);
+
+/* Point sources for fdtd_run: after the E update of step t, E[index[k]] += values[t*n + k]
+ * (the host-side `sim.E[ind] += field_source(t)` of opencl_fdtd's fdtd.py:168-169, moved on
+ * the device). index is a flat index into the 3N E array; values is a device array of
+ * nsteps*n elements in the plan's dtype. */
+typedef struct FdtdPointSources {
+    int32_t n;
+    int32_t _pad;
+    const int64_t *index;    /* device, n entries */
+    const void *values;      /* device, nsteps * n entries */
+} FdtdPointSources;
+
+/* Run nsteps canonical steps (fdtd.py:162-175: E, F, point sources, H, G, S) on the stream
+ * with no host round trip. src may be NULL. */
+int fdtd_run(FdtdPlan *plan, const FdtdBuffers *buf, void *stream, int32_t nsteps,
+             const FdtdPointSources *src);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FDTD_GB300_H */

@@ -1,0 +1,120 @@
+"""
+ctypes binding of the C ABI declared in include/fdtd_gb300.h.
+
+The structures below mirror the header field for field; tests compare their sizes and
+offsets with what a C compiler reports for the header. Loading fails loudly when the
+library is not built: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+c_i32, c_i64, c_f64, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
+
+FDTD_OK = 0
+FDTD_ERR_INVALID = -1
+FDTD_ERR_UNSUPPORTED = -2
+FDTD_ERR_CUDA = -3
+FDTD_ERR_WATCHDOG = -4
+FDTD_ERR_NONFINITE = -5
+FDTD_F32 = 0
+FDTD_F64 = 1
+
+
+class FdtdPmlDesc(ctypes.Structure):
+    _fields_ = [("axis", c_i32), ("polarity", c_i32), ("thickness", c_i32), ("_pad", c_i32),
+                ("p0e", c_vp), ("p1e", c_vp), ("p2e", c_vp),
+                ("p0h", c_vp), ("p1h", c_vp), ("p2h", c_vp)]
+
+
+class FdtdBlochDesc(ctypes.Structure):
+    _fields_ = [("axis", c_i32), ("_pad", c_i32), ("real", c_f64), ("imag", c_f64)]
+
+
+class FdtdDesc(ctypes.Structure):
+    _fields_ = [("shape", c_i64 * 3), ("dtype", c_i32), ("uniform", c_i32),
+                ("dt", c_f64), ("dx", c_f64),
+                ("n_pml", c_i32), ("n_bloch", c_i32),
+                ("pml", FdtdPmlDesc * 6), ("bloch", FdtdBlochDesc * 3),
+                ("do_poynting", c_i32), ("do_fieldsrc", c_i32), ("has_mu", c_i32), ("_pad", c_i32)]
+
+
+_PSI = (c_vp * 2) * 6
+
+
+class FdtdBuffers(ctypes.Structure):
+    _fields_ = [("E", c_vp), ("H", c_vp), ("F", c_vp), ("G", c_vp),
+                ("eps", c_vp), ("mu", c_vp), ("S", c_vp), ("oS", c_vp),
+                ("Jr", c_vp), ("Ji", c_vp),
+                ("psi_e", _PSI), ("psi_h", _PSI), ("psi_f", _PSI), ("psi_g", _PSI),
+                ("inv_de", c_vp * 3), ("inv_dh", c_vp * 3)]
+
+
+class FdtdPointSources(ctypes.Structure):
+    _fields_ = [("n", c_i32), ("_pad", c_i32), ("index", c_vp), ("values", c_vp)]
+
+
+# (name, restype, argtypes) of every entry point in include/fdtd_gb300.h
+_P = ctypes.POINTER
+SIGNATURES = [
+    ("fdtd_abi_version", c_i32, []),
+    ("fdtd_last_error", ctypes.c_char_p, []),
+    ("fdtd_plan_create", c_i32, [_P(FdtdDesc), _P(c_vp)]),
+    ("fdtd_plan_destroy", c_i32, [c_vp]),
+    ("fdtd_update_e", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),
+    ("fdtd_update_h", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),
+    ("fdtd_update_s", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),
+    ("fdtd_update_f", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),
+    ("fdtd_update_g", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),
+    ("fdtd_update_j", c_i32, [c_vp, _P(FdtdBuffers), c_vp, c_f64, c_f64, _P(c_i64)]),
+    ("fdtd_run", c_i32, [c_vp, _P(FdtdBuffers), c_vp, c_i32, _P(FdtdPointSources)]),
+]
+
+_LIB = None
+_LOCK = threading.Lock()
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(auto_build: bool = True):
+    """Load libfdtd_gb300.so (building it first when nvcc is available)."""
+    global _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = _build.LIB
+        if auto_build:
+            try:
+                _build.build()
+            except RuntimeError as e:
+                if not os.path.exists(path):
+                    raise RuntimeError("libfdtd_gb300.so is not built and the build failed: %s" % e)
+        if not os.path.exists(path):
+            raise RuntimeError("libfdtd_gb300.so is not built (run opencl_fdtd_gb300.build.build())")
+        lib = ctypes.CDLL(path)
+        for name, res, args in SIGNATURES:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if lib.fdtd_abi_version() != 1:
+            raise RuntimeError("libfdtd_gb300.so ABI version mismatch")
+        _LIB = lib
+        return lib
+
+
+class FdtdError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s (status %d)" % (msg, code))
+        self.code = code
+
+
+def check(rc: int):
+    if rc != FDTD_OK:
+        msg = load().fdtd_last_error().decode(errors="replace")
+        raise FdtdError(rc, msg)

@@ -1,0 +1,431 @@
+// C ABI of the FDTD library (include/fdtd_gb300.h): plans, validation and launch dispatch.
+//
+// A plan stands in for what opencl_fdtd's Simulation.__init__ bakes into its rendered kernel
+// sources (opencl_fdtd/simulation.py:170-271): grid shape, dtype, spacing, the CPML face list
+// with its coefficient tables (simulation.py:274-319), Bloch phases and the Poynting/field-
+// source switches. The kernels are compiled once for every combination instead of being
+// rendered per simulation; the plan only fills their argument blocks.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fdtd_gb300.h"
+#include "yee_common.cuh"
+#include "yee_launch.h"
+#include "fdtd_plan.h"
+
+using namespace fdtd;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return FDTD_ERR_CUDA;
+}
+
+}  // namespace
+
+namespace fdtd {
+
+int set_error(int code, const char *msg)
+{
+    return fail(code, msg);
+}
+
+int check_cuda(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return FDTD_OK;
+    return cuda_fail(e, what);
+}
+
+// Bloch factors as each update reads them (see k_yee_e / k_yee_h): E-type real part uses
+// +imag, imaginary part -imag; H-type real part -imag, imaginary part +imag.
+template <typename R>
+YeeK<R> make_yee(const FdtdPlan *p, bool etype, bool imag, R *P, const R *Q, const R *Rp,
+                 const R *mat, R *oS, void *const psi[6][2], const void *const inv_tab[3])
+{
+    YeeK<R> k;
+    std::memset(&k, 0, sizeof(k));
+    k.P = P;
+    k.Q = Q;
+    k.Rp = Rp;
+    k.mat = mat;
+    k.oS = oS;
+    k.sx = p->sx;
+    k.sy = p->sy;
+    k.sz = p->sz;
+    k.syz = p->syz;
+    k.N = p->N;
+    k.dsz = FastDiv::make(p->sz);
+    k.dt = (R)p->d.dt;
+    k.inv_d = (R)(1.0 / p->d.dx);
+    for (int r = 0; r < 3; ++r) k.inv_tab[r] = p->d.uniform ? nullptr : (const R *)inv_tab[r];
+    k.nface = p->d.n_pml;
+    for (int f = 0; f < p->d.n_pml; ++f) {
+        const FdtdPmlDesc &pd = p->d.pml[f];
+        FaceK<R> &fk = k.face[f];
+        fk.axis = pd.axis;
+        fk.pol = pd.polarity;
+        fk.T = pd.thickness;
+        const int base = etype ? 0 : 3;
+        fk.p0 = (const R *)p->tab[f][base + 0];
+        fk.p1 = (const R *)p->tab[f][base + 1];
+        fk.p2 = (const R *)p->tab[f][base + 2];
+        fk.psi_u = (R *)psi[f][0];
+        fk.psi_v = (R *)psi[f][1];
+    }
+    k.bloch_mask = 0;
+    for (int r = 0; r < 3; ++r) {
+        k.br[r] = R(1);
+        k.bi[r] = R(0);
+    }
+    if (Rp) {
+        for (int b = 0; b < p->d.n_bloch; ++b) {
+            const FdtdBlochDesc &bd = p->d.bloch[b];
+            k.bloch_mask |= 1 << bd.axis;
+            k.br[bd.axis] = (R)bd.real;
+            const bool plus = etype ? !imag : imag;
+            k.bi[bd.axis] = (R)(plus ? bd.imag : -bd.imag);
+        }
+    }
+    return k;
+}
+
+template <typename R>
+int run_update_e(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag)
+{
+    R *P = (R *)(imag ? b->F : b->E);
+    const R *Q = (const R *)(imag ? b->G : b->H);
+    const R *Rp = p->d.n_bloch ? (const R *)(imag ? b->H : b->G) : nullptr;
+    void *const(*psi)[2] = imag ? b->psi_f : b->psi_e;
+    YeeK<R> k = make_yee<R>(p, true, imag, P, Q, Rp, (const R *)b->eps, nullptr, psi, b->inv_dh);
+    return check_cuda(launch_yee_e<R>(k, st), imag ? "update_F launch" : "update_E launch");
+}
+
+template <typename R>
+int run_update_h(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag)
+{
+    R *P = (R *)(imag ? b->G : b->H);
+    const R *Q = (const R *)(imag ? b->F : b->E);
+    const R *Rp = p->d.n_bloch ? (const R *)(imag ? b->E : b->F) : nullptr;
+    void *const(*psi)[2] = imag ? b->psi_g : b->psi_h;
+    const bool poynt = p->d.do_poynting && !imag;
+    YeeK<R> k = make_yee<R>(p, false, imag, P, Q, Rp, p->d.has_mu ? (const R *)b->mu : nullptr,
+                            poynt ? (R *)b->oS : nullptr, psi, b->inv_de);
+    return check_cuda(launch_yee_h<R>(k, p->d.has_mu != 0, poynt, st),
+                      imag ? "update_G launch" : "update_H launch");
+}
+
+template <typename R>
+int run_update_s(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st)
+{
+    SK<R> k;
+    k.S = (R *)b->S;
+    k.oS = (const R *)b->oS;
+    k.sx = p->sx;
+    k.sy = p->sy;
+    k.sz = p->sz;
+    k.syz = p->syz;
+    k.N = p->N;
+    k.dsz = FastDiv::make(p->sz);
+    const R dt = (R)p->d.dt;
+    k.sf = (R)((double)dt * 0.125);  // update_s.cl:33
+    return check_cuda(launch_poynting<R>(k, st), "update_S launch");
+}
+
+template <typename R>
+int run_update_j(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, double c, double s,
+                 const uint32_t lo[3], const uint32_t n[3])
+{
+    JK<R> k;
+    k.E = (R *)b->E;
+    k.Jr = (const R *)b->Jr;
+    k.Ji = (const R *)b->Ji;
+    k.sy = p->sy;
+    k.sz = p->sz;
+    k.N = p->N;
+    k.x0 = lo[0];
+    k.y0 = lo[1];
+    k.z0 = lo[2];
+    k.nx = n[0];
+    k.ny = n[1];
+    k.nz = n[2];
+    k.dnz = FastDiv::make(n[2] ? n[2] : 1);
+    k.dnyz = FastDiv::make(n[1] * n[2] ? n[1] * n[2] : 1);
+    k.c = (R)c;
+    k.s = (R)s;
+    return check_cuda(launch_fieldsrc<R>(k, st), "update_J launch");
+}
+
+template <typename R>
+int run_point_sources(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st,
+                      const FdtdPointSources *src, int t)
+{
+    PointK<R> k;
+    k.E = (R *)b->E;
+    k.index = src->index;
+    k.values = (const R *)src->values;
+    k.n = src->n;
+    k.t = t;
+    return check_cuda(launch_point_sources<R>(k, st), "point source launch");
+}
+
+}  // namespace fdtd
+
+// ---------------------------------------------------------------------------------------------
+// validation
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+int validate_desc(const FdtdDesc *d)
+{
+    if (!d) return fail(FDTD_ERR_INVALID, "desc is NULL");
+    for (int r = 0; r < 3; ++r)
+        if (d->shape[r] < 1) return fail(FDTD_ERR_INVALID, "shape entries must be >= 1");
+    const unsigned long long N = (unsigned long long)d->shape[0] * d->shape[1] * d->shape[2];
+    if (N >= (1ull << 32)) return fail(FDTD_ERR_INVALID, "grid too large: N must be < 2^32 cells");
+    if (d->shape[0] > 65535) return fail(FDTD_ERR_INVALID, "sx must be <= 65535");
+    if (d->dtype != FDTD_F32 && d->dtype != FDTD_F64)
+        return fail(FDTD_ERR_UNSUPPORTED, "dtype must be FDTD_F32 or FDTD_F64");
+    if (!(d->dt > 0)) return fail(FDTD_ERR_INVALID, "dt must be > 0");
+    if (d->uniform && !(d->dx > 0)) return fail(FDTD_ERR_INVALID, "dx must be > 0");
+    if (d->n_pml < 0 || d->n_pml > 6) return fail(FDTD_ERR_INVALID, "n_pml must be in [0, 6]");
+    int seen = 0;
+    for (int f = 0; f < d->n_pml; ++f) {
+        const FdtdPmlDesc &p = d->pml[f];
+        if (p.axis < 0 || p.axis > 2) return fail(FDTD_ERR_INVALID, "pml axis must be 0, 1 or 2");
+        if (p.polarity != 0 && p.polarity != 1)
+            return fail(FDTD_ERR_INVALID, "pml polarity must be 0 ('n') or 1 ('p')");
+        if (p.thickness < 0 || p.thickness > 65535)
+            return fail(FDTD_ERR_INVALID, "pml thickness must be in [0, 65535]");
+        const int bit = 1 << (2 * p.axis + p.polarity);
+        if (seen & bit) return fail(FDTD_ERR_INVALID, "duplicate pml face");
+        seen |= bit;
+        if (p.thickness > 0 && (!p.p0e || !p.p1e || !p.p2e || !p.p0h || !p.p1h || !p.p2h))
+            return fail(FDTD_ERR_INVALID, "pml coefficient table pointer is NULL");
+    }
+    if (d->n_bloch < 0 || d->n_bloch > 3) return fail(FDTD_ERR_INVALID, "n_bloch must be in [0, 3]");
+    int bseen = 0;
+    for (int b = 0; b < d->n_bloch; ++b) {
+        const int a = d->bloch[b].axis;
+        if (a < 0 || a > 2) return fail(FDTD_ERR_INVALID, "bloch axis must be 0, 1 or 2");
+        if (bseen & (1 << a)) return fail(FDTD_ERR_INVALID, "duplicate bloch axis");
+        bseen |= 1 << a;
+    }
+    return FDTD_OK;
+}
+
+int check_common(const FdtdPlan *p, const FdtdBuffers *b)
+{
+    if (!p) return fail(FDTD_ERR_INVALID, "plan is NULL");
+    if (!b) return fail(FDTD_ERR_INVALID, "buffers is NULL");
+    return FDTD_OK;
+}
+
+int check_psi(const FdtdPlan *p, void *const psi[6][2], const char *what)
+{
+    for (int f = 0; f < p->d.n_pml; ++f)
+        if (p->d.pml[f].thickness > 0 && (!psi[f][0] || !psi[f][1]))
+            return fail(FDTD_ERR_INVALID, std::string(what) + ": psi pointer is NULL");
+    return FDTD_OK;
+}
+
+int check_inv(const FdtdPlan *p, const void *const inv[3], const char *what)
+{
+    if (p->d.uniform) return FDTD_OK;
+    for (int r = 0; r < 3; ++r)
+        if (!inv[r]) return fail(FDTD_ERR_INVALID, std::string(what) + ": spacing table is NULL");
+    return FDTD_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// extern "C" entry points
+// ---------------------------------------------------------------------------------------------
+extern "C" {
+
+int fdtd_abi_version(void) { return FDTD_ABI_VERSION; }
+
+const char *fdtd_last_error(void) { return g_err.c_str(); }
+
+int fdtd_plan_create(const FdtdDesc *desc, FdtdPlan **out)
+{
+    if (!out) return fail(FDTD_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    int rc = validate_desc(desc);
+    if (rc) return rc;
+    FdtdPlan *p = new FdtdPlan();
+    p->d = *desc;
+    p->sx = (uint32_t)desc->shape[0];
+    p->sy = (uint32_t)desc->shape[1];
+    p->sz = (uint32_t)desc->shape[2];
+    p->syz = p->sy * p->sz;
+    p->N = (uint64_t)p->sx * p->syz;
+    p->elem = desc->dtype == FDTD_F64 ? 8 : 4;
+    cudaGetDevice(&p->device);
+    size_t total = 0;
+    for (int f = 0; f < desc->n_pml; ++f) total += 6 * (size_t)desc->pml[f].thickness;
+    std::memset(p->tab, 0, sizeof(p->tab));
+    if (total) {
+        cudaError_t e = cudaMalloc(&p->coef, total * p->elem);
+        if (e != cudaSuccess) {
+            delete p;
+            return cuda_fail(e, "cudaMalloc(coefficient tables)");
+        }
+        std::vector<char> host(total * p->elem);
+        size_t off = 0;
+        for (int f = 0; f < desc->n_pml; ++f) {
+            const FdtdPmlDesc &pd = desc->pml[f];
+            const size_t bytes = (size_t)pd.thickness * p->elem;
+            const void *src[6] = {pd.p0e, pd.p1e, pd.p2e, pd.p0h, pd.p1h, pd.p2h};
+            for (int t = 0; t < 6; ++t) {
+                if (bytes) std::memcpy(host.data() + off, src[t], bytes);
+                p->tab[f][t] = (char *)p->coef + off;
+                off += bytes;
+            }
+        }
+        e = cudaMemcpy(p->coef, host.data(), host.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(p->coef);
+            delete p;
+            return cuda_fail(e, "cudaMemcpy(coefficient tables)");
+        }
+    }
+    *out = p;
+    g_err.clear();
+    return FDTD_OK;
+}
+
+int fdtd_plan_destroy(FdtdPlan *plan)
+{
+    if (!plan) return FDTD_OK;
+    if (plan->coef) cudaFree(plan->coef);
+    delete plan;
+    return FDTD_OK;
+}
+
+int fdtd_update_e(FdtdPlan *p, const FdtdBuffers *b, void *stream)
+{
+    int rc = check_common(p, b);
+    if (rc) return rc;
+    if (!b->E || !b->H || !b->eps) return fail(FDTD_ERR_INVALID, "update_E: E, H and eps are required");
+    if (p->d.n_bloch && !b->G) return fail(FDTD_ERR_INVALID, "update_E: G is required with Bloch boundaries");
+    if ((rc = check_psi(p, b->psi_e, "update_E"))) return rc;
+    if ((rc = check_inv(p, b->inv_dh, "update_E"))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == FDTD_F64 ? run_update_e<double>(p, b, st, false)
+                                  : run_update_e<float>(p, b, st, false);
+}
+
+int fdtd_update_f(FdtdPlan *p, const FdtdBuffers *b, void *stream)
+{
+    int rc = check_common(p, b);
+    if (rc) return rc;
+    if (!p->d.n_bloch) return fail(FDTD_ERR_INVALID, "update_F: the plan has no Bloch boundaries");
+    if (!b->F || !b->G || !b->H || !b->eps)
+        return fail(FDTD_ERR_INVALID, "update_F: F, G, H and eps are required");
+    if ((rc = check_psi(p, b->psi_f, "update_F"))) return rc;
+    if ((rc = check_inv(p, b->inv_dh, "update_F"))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == FDTD_F64 ? run_update_e<double>(p, b, st, true)
+                                  : run_update_e<float>(p, b, st, true);
+}
+
+int fdtd_update_h(FdtdPlan *p, const FdtdBuffers *b, void *stream)
+{
+    int rc = check_common(p, b);
+    if (rc) return rc;
+    if (!b->E || !b->H) return fail(FDTD_ERR_INVALID, "update_H: E and H are required");
+    if (p->d.n_bloch && !b->F) return fail(FDTD_ERR_INVALID, "update_H: F is required with Bloch boundaries");
+    if (p->d.has_mu && !b->mu) return fail(FDTD_ERR_INVALID, "update_H: mu is required");
+    if (p->d.do_poynting && !b->oS) return fail(FDTD_ERR_INVALID, "update_H: oS is required with Poynting");
+    if ((rc = check_psi(p, b->psi_h, "update_H"))) return rc;
+    if ((rc = check_inv(p, b->inv_de, "update_H"))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == FDTD_F64 ? run_update_h<double>(p, b, st, false)
+                                  : run_update_h<float>(p, b, st, false);
+}
+
+int fdtd_update_g(FdtdPlan *p, const FdtdBuffers *b, void *stream)
+{
+    int rc = check_common(p, b);
+    if (rc) return rc;
+    if (!p->d.n_bloch) return fail(FDTD_ERR_INVALID, "update_G: the plan has no Bloch boundaries");
+    if (!b->F || !b->G || !b->E) return fail(FDTD_ERR_INVALID, "update_G: E, F and G are required");
+    if (p->d.has_mu && !b->mu) return fail(FDTD_ERR_INVALID, "update_G: mu is required");
+    if ((rc = check_psi(p, b->psi_g, "update_G"))) return rc;
+    if ((rc = check_inv(p, b->inv_de, "update_G"))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == FDTD_F64 ? run_update_h<double>(p, b, st, true)
+                                  : run_update_h<float>(p, b, st, true);
+}
+
+int fdtd_update_s(FdtdPlan *p, const FdtdBuffers *b, void *stream)
+{
+    int rc = check_common(p, b);
+    if (rc) return rc;
+    if (!p->d.do_poynting) return fail(FDTD_ERR_INVALID, "update_S: the plan has Poynting off");
+    if (!b->S || !b->oS) return fail(FDTD_ERR_INVALID, "update_S: S and oS are required");
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == FDTD_F64 ? run_update_s<double>(p, b, st) : run_update_s<float>(p, b, st);
+}
+
+int fdtd_update_j(FdtdPlan *p, const FdtdBuffers *b, void *stream, double c, double s,
+                  const int64_t box[6])
+{
+    int rc = check_common(p, b);
+    if (rc) return rc;
+    if (!p->d.do_fieldsrc) return fail(FDTD_ERR_INVALID, "update_J: the plan has the field source off");
+    if (!b->E || !b->Jr || !b->Ji) return fail(FDTD_ERR_INVALID, "update_J: E, Jr and Ji are required");
+    if (!box) return fail(FDTD_ERR_INVALID, "update_J: box is NULL");
+    const int64_t s3[3] = {(int64_t)p->sx, (int64_t)p->sy, (int64_t)p->sz};
+    uint32_t lo[3], n[3];
+    for (int r = 0; r < 3; ++r) {
+        const int64_t a = box[2 * r], e = box[2 * r + 1];
+        if (a < 0 || e < 0 || a > 0xffffffffll || e > 0xffffffffll)
+            return fail(FDTD_ERR_INVALID, "update_J: box bounds must be unsigned 32-bit values");
+        const int64_t ec = e < s3[r] ? e : s3[r];
+        lo[r] = (uint32_t)a;
+        n[r] = ec > a ? (uint32_t)(ec - a) : 0u;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == FDTD_F64 ? run_update_j<double>(p, b, st, c, s, lo, n)
+                                  : run_update_j<float>(p, b, st, c, s, lo, n);
+}
+
+int fdtd_run(FdtdPlan *p, const FdtdBuffers *b, void *stream, int32_t nsteps,
+             const FdtdPointSources *src)
+{
+    int rc = check_common(p, b);
+    if (rc) return rc;
+    if (nsteps < 0) return fail(FDTD_ERR_INVALID, "fdtd_run: nsteps must be >= 0");
+    if (src && src->n > 0 && (!src->index || !src->values))
+        return fail(FDTD_ERR_INVALID, "fdtd_run: source index/values pointer is NULL");
+    const bool f64 = p->d.dtype == FDTD_F64;
+    for (int t = 0; t < nsteps; ++t) {
+        if ((rc = fdtd_update_e(p, b, stream))) return rc;
+        if (p->d.n_bloch && (rc = fdtd_update_f(p, b, stream))) return rc;
+        if (src && src->n > 0) {
+            rc = f64 ? run_point_sources<double>(p, b, (cudaStream_t)stream, src, t)
+                     : run_point_sources<float>(p, b, (cudaStream_t)stream, src, t);
+            if (rc) return rc;
+        }
+        if ((rc = fdtd_update_h(p, b, stream))) return rc;
+        if (p->d.n_bloch && (rc = fdtd_update_g(p, b, stream))) return rc;
+        if (p->d.do_poynting && (rc = fdtd_update_s(p, b, stream))) return rc;
+    }
+    return FDTD_OK;
+}
+
+}  // extern "C"

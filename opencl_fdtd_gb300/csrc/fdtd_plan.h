@@ -1,0 +1,22 @@
+// Host-side plan object behind the opaque FdtdPlan of include/fdtd_gb300.h.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include "fdtd_gb300.h"
+
+struct FdtdPlan {
+    FdtdDesc d;                 // copy of the caller's description
+    uint32_t sx, sy, sz, syz;
+    uint64_t N;
+    size_t elem;                // bytes per element of the plan's dtype
+    int device;                 // device that was current at creation
+    void *coef = nullptr;       // device copy of every face's six coefficient tables
+    const void *tab[6][6];      // per face: p0e p1e p2e p0h p1h p2h (device pointers)
+};
+
+namespace fdtd {
+int set_error(int code, const char *msg);
+int check_cuda(cudaError_t e, const char *what);
+}  // namespace fdtd

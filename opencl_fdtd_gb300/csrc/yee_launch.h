@@ -1,0 +1,14 @@
+// Host-side launchers of the Yee kernels (defined in yee_kernels.cu).
+#pragma once
+
+#include "yee_common.cuh"
+
+namespace fdtd {
+
+template <typename R> cudaError_t launch_yee_e(const YeeK<R> &k, cudaStream_t st);
+template <typename R> cudaError_t launch_yee_h(const YeeK<R> &k, bool mu, bool poynting, cudaStream_t st);
+template <typename R> cudaError_t launch_poynting(const SK<R> &k, cudaStream_t st);
+template <typename R> cudaError_t launch_fieldsrc(const JK<R> &k, cudaStream_t st);
+template <typename R> cudaError_t launch_point_sources(const PointK<R> &k, cudaStream_t st);
+
+}  // namespace fdtd
