@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--xchunk", type=int, default=0, help="x planes per thread (0: plan default)")
     return ap.parse_args()
 
 
@@ -224,6 +225,8 @@ def main():
     wl = workloads.get(args.workload)
     kw = wl["kwargs"]
     sim = Simulation(**kw)
+    if args.xchunk:
+        _lib.check(sim._lib.fdtd_plan_tune(sim._plan, args.xchunk))
     N = int(numpy.prod(wl["shape"]))
     fc = workloads.face_cells(wl["shape"], kw["pmls"])
     poynting = kw.get("do_poynting", True)

@@ -91,6 +91,10 @@ typedef struct FdtdBuffers {
     /* non-uniform spacing: 1/dx on the E grid (H updates read these) and on the H grid
      * (E updates read these), lengths sx, sy, sz; NULL when uniform */
     const void *inv_de[3], *inv_dh[3];
+    /* Optional 3N caches of dt/eps and dt/mu (the per-cell quotient of update_e.cl:105-107),
+     * filled by fdtd_prepare. When set they must be current; when NULL every cell divides,
+     * which is slower but gives the same result. */
+    void *ce, *cm;
 } FdtdBuffers;
 
 typedef struct FdtdPlan FdtdPlan;
@@ -105,6 +109,14 @@ const char *fdtd_last_error(void);
  * Replaces Simulation.__init__'s kernel generation (simulation.py:170-271). */
 int fdtd_plan_create(const FdtdDesc *desc, FdtdPlan **out);
 int fdtd_plan_destroy(FdtdPlan *plan);
+
+/* Tuning: number of consecutive x planes one thread of the update kernels advances
+ * (default 16). Any value gives the same results. */
+int fdtd_plan_tune(FdtdPlan *plan, int32_t xchunk);
+
+/* Fill buf->ce = dt/eps and, with has_mu, buf->cm = dt/mu (IEEE division, the quotient
+ * the reference computes per cell). Call after creating or changing eps/mu. */
+int fdtd_prepare(FdtdPlan *plan, const FdtdBuffers *buf, void *stream);
 
 /* update_E (simulation.py:254; opencl_fdtd/kernels/update_e.cl): E += dt/eps * (curl H + psi),
  * advancing psi_e. With Bloch boundaries it reads G at the wrapped faces. */

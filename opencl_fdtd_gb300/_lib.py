@@ -51,7 +51,8 @@ class FdtdBuffers(ctypes.Structure):
                 ("eps", c_vp), ("mu", c_vp), ("S", c_vp), ("oS", c_vp),
                 ("Jr", c_vp), ("Ji", c_vp),
                 ("psi_e", _PSI), ("psi_h", _PSI), ("psi_f", _PSI), ("psi_g", _PSI),
-                ("inv_de", c_vp * 3), ("inv_dh", c_vp * 3)]
+                ("inv_de", c_vp * 3), ("inv_dh", c_vp * 3),
+                ("ce", c_vp), ("cm", c_vp)]
 
 
 class FdtdPointSources(ctypes.Structure):
@@ -65,6 +66,8 @@ SIGNATURES = [
     ("fdtd_last_error", ctypes.c_char_p, []),
     ("fdtd_plan_create", c_i32, [_P(FdtdDesc), _P(c_vp)]),
     ("fdtd_plan_destroy", c_i32, [c_vp]),
+    ("fdtd_plan_tune", c_i32, [c_vp, c_i32]),
+    ("fdtd_prepare", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),
     ("fdtd_update_e", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),
     ("fdtd_update_h", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),
     ("fdtd_update_s", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),

@@ -48,11 +48,29 @@ int check_cuda(cudaError_t e, const char *what)
     return cuda_fail(e, what);
 }
 
-// Bloch factors as each update reads them (see k_yee_e / k_yee_h): E-type real part uses
+// True when no two CPML faces of one axis share a cell, so every cell sees at most one face
+// per axis and the bulk kernels (which apply faces per axis) match the list order exactly.
+bool faces_disjoint(const FdtdPlan *p)
+{
+    const uint32_t s[3] = {p->sx, p->sy, p->sz};
+    uint32_t tn[3] = {0, 0, 0}, tp[3] = {0, 0, 0};
+    for (int f = 0; f < p->d.n_pml; ++f) {
+        const FdtdPmlDesc &pd = p->d.pml[f];
+        const uint32_t T = (uint32_t)pd.thickness, a = (uint32_t)pd.axis;
+        if (pd.polarity == 0) tn[a] = T;
+        else if (T <= s[a]) tp[a] = T;
+    }
+    for (int r = 0; r < 3; ++r)
+        if ((uint64_t)tn[r] + tp[r] > s[r]) return false;
+    return true;
+}
+
+// Bloch factors as each update reads them (see cell_e / cell_h in yee_kernels.cu): E-type real part uses
 // +imag, imaginary part -imag; H-type real part -imag, imaginary part +imag.
 template <typename R>
 YeeK<R> make_yee(const FdtdPlan *p, bool etype, bool imag, R *P, const R *Q, const R *Rp,
-                 const R *mat, R *oS, void *const psi[6][2], const void *const inv_tab[3])
+                 const R *mat, const R *coef, R *oS, void *const psi[6][2],
+                 const void *const inv_tab[3])
 {
     YeeK<R> k;
     std::memset(&k, 0, sizeof(k));
@@ -60,13 +78,18 @@ YeeK<R> make_yee(const FdtdPlan *p, bool etype, bool imag, R *P, const R *Q, con
     k.Q = Q;
     k.Rp = Rp;
     k.mat = mat;
+    k.coef = coef;
     k.oS = oS;
+    k.dxmode = !p->d.uniform ? 2 : ((R)(1.0 / p->d.dx) == R(1) ? 0 : 1);
+    const bool coef_ok = etype ? coef != nullptr : (mat == nullptr || coef != nullptr);
+    k.bulk = coef_ok && faces_disjoint(p);
+    k.xchunk = p->xchunk;
+    k.dsz = FastDiv::make(p->sz);
     k.sx = p->sx;
     k.sy = p->sy;
     k.sz = p->sz;
     k.syz = p->syz;
     k.N = p->N;
-    k.dsz = FastDiv::make(p->sz);
     k.dt = (R)p->d.dt;
     k.inv_d = (R)(1.0 / p->d.dx);
     for (int r = 0; r < 3; ++r) k.inv_tab[r] = p->d.uniform ? nullptr : (const R *)inv_tab[r];
@@ -83,6 +106,17 @@ YeeK<R> make_yee(const FdtdPlan *p, bool etype, bool imag, R *P, const R *Q, con
         fk.p2 = (const R *)p->tab[f][base + 2];
         fk.psi_u = (R *)psi[f][0];
         fk.psi_v = (R *)psi[f][1];
+        AxisK<R> &ak = k.ax[pd.axis];
+        const uint32_t sa = pd.axis == 0 ? p->sx : pd.axis == 1 ? p->sy : p->sz;
+        if (pd.polarity == 0) {
+            ak.Tn = pd.thickness;
+            ak.n0 = fk.p0; ak.n1 = fk.p1; ak.n2 = fk.p2;
+            ak.nu = fk.psi_u; ak.nv = fk.psi_v;
+        } else if ((uint32_t)pd.thickness <= sa) {
+            ak.Tp = pd.thickness;
+            ak.p0 = fk.p0; ak.p1 = fk.p1; ak.p2 = fk.p2;
+            ak.pu = fk.psi_u; ak.pv = fk.psi_v;
+        }
     }
     k.bloch_mask = 0;
     for (int r = 0; r < 3; ++r) {
@@ -108,7 +142,8 @@ int run_update_e(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag)
     const R *Q = (const R *)(imag ? b->G : b->H);
     const R *Rp = p->d.n_bloch ? (const R *)(imag ? b->H : b->G) : nullptr;
     void *const(*psi)[2] = imag ? b->psi_f : b->psi_e;
-    YeeK<R> k = make_yee<R>(p, true, imag, P, Q, Rp, (const R *)b->eps, nullptr, psi, b->inv_dh);
+    YeeK<R> k = make_yee<R>(p, true, imag, P, Q, Rp, (const R *)b->eps, (const R *)b->ce, nullptr,
+                            psi, b->inv_dh);
     return check_cuda(launch_yee_e<R>(k, st), imag ? "update_F launch" : "update_E launch");
 }
 
@@ -121,6 +156,7 @@ int run_update_h(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag)
     void *const(*psi)[2] = imag ? b->psi_g : b->psi_h;
     const bool poynt = p->d.do_poynting && !imag;
     YeeK<R> k = make_yee<R>(p, false, imag, P, Q, Rp, p->d.has_mu ? (const R *)b->mu : nullptr,
+                            p->d.has_mu ? (const R *)b->cm : nullptr,
                             poynt ? (R *)b->oS : nullptr, psi, b->inv_de);
     return check_cuda(launch_yee_h<R>(k, p->d.has_mu != 0, poynt, st),
                       imag ? "update_G launch" : "update_H launch");
@@ -130,6 +166,7 @@ template <typename R>
 int run_update_s(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st)
 {
     SK<R> k;
+    std::memset(&k, 0, sizeof(k));
     k.S = (R *)b->S;
     k.oS = (const R *)b->oS;
     k.sx = p->sx;
@@ -138,9 +175,30 @@ int run_update_s(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st)
     k.syz = p->syz;
     k.N = p->N;
     k.dsz = FastDiv::make(p->sz);
+    k.xchunk = p->xchunk;
     const R dt = (R)p->d.dt;
     k.sf = (R)((double)dt * 0.125);  // update_s.cl:33
     return check_cuda(launch_poynting<R>(k, st), "update_S launch");
+}
+
+template <typename R>
+int run_prepare(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st)
+{
+    PrepK<R> k;
+    k.n = 3 * p->N;
+    k.dt = (R)p->d.dt;
+    if (b->ce) {
+        k.out = (R *)b->ce;
+        k.mat = (const R *)b->eps;
+        int rc = check_cuda(launch_prepare<R>(k, st), "prepare(dt/eps) launch");
+        if (rc) return rc;
+    }
+    if (p->d.has_mu && b->cm) {
+        k.out = (R *)b->cm;
+        k.mat = (const R *)b->mu;
+        return check_cuda(launch_prepare<R>(k, st), "prepare(dt/mu) launch");
+    }
+    return FDTD_OK;
 }
 
 template <typename R>
@@ -273,6 +331,7 @@ int fdtd_plan_create(const FdtdDesc *desc, FdtdPlan **out)
     p->syz = p->sy * p->sz;
     p->N = (uint64_t)p->sx * p->syz;
     p->elem = desc->dtype == FDTD_F64 ? 8 : 4;
+    p->xchunk = 16;
     cudaGetDevice(&p->device);
     size_t total = 0;
     for (int f = 0; f < desc->n_pml; ++f) total += 6 * (size_t)desc->pml[f].thickness;
@@ -313,6 +372,24 @@ int fdtd_plan_destroy(FdtdPlan *plan)
     if (plan->coef) cudaFree(plan->coef);
     delete plan;
     return FDTD_OK;
+}
+
+int fdtd_plan_tune(FdtdPlan *p, int32_t xchunk)
+{
+    if (!p) return fail(FDTD_ERR_INVALID, "plan is NULL");
+    if (xchunk < 1 || xchunk > 4096) return fail(FDTD_ERR_INVALID, "xchunk must be in [1, 4096]");
+    p->xchunk = xchunk;
+    return FDTD_OK;
+}
+
+int fdtd_prepare(FdtdPlan *p, const FdtdBuffers *b, void *stream)
+{
+    int rc = check_common(p, b);
+    if (rc) return rc;
+    if (b->ce && !b->eps) return fail(FDTD_ERR_INVALID, "prepare: eps is required to fill ce");
+    if (p->d.has_mu && b->cm && !b->mu) return fail(FDTD_ERR_INVALID, "prepare: mu is required to fill cm");
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == FDTD_F64 ? run_prepare<double>(p, b, st) : run_prepare<float>(p, b, st);
 }
 
 int fdtd_update_e(FdtdPlan *p, const FdtdBuffers *b, void *stream)

@@ -12,6 +12,7 @@ struct FdtdPlan {
     uint64_t N;
     size_t elem;                // bytes per element of the plan's dtype
     int device;                 // device that was current at creation
+    int32_t xchunk;             // x planes a bulk-kernel thread marches
     void *coef = nullptr;       // device copy of every face's six coefficient tables
     const void *tab[6][6];      // per face: p0e p1e p2e p0h p1h p2h (device pointers)
 };

@@ -3,6 +3,11 @@
 // Grid and field layout follow opencl_fdtd/kernels/common.cl:34-52: a field is [X | Y | Z],
 // each component C-ordered (x, y, z) with z fastest, so cell (x, y, z) is flat index
 // i = (x*sy + y)*sz + z and the component offsets are 0, N, 2N.
+//
+// Every update is one "bulk" launch: thread (y, z) of a plane marches a chunk of
+// consecutive x planes. The generic per-cell kernels (faces applied in list order) remain
+// for the one case the bulk kernels exclude: two CPML faces of one axis that overlap.
+// Both apply the same per-cell arithmetic.
 #pragma once
 
 #include <cstdint>
@@ -17,11 +22,11 @@ struct FastDiv {
     static FastDiv make(uint32_t dd)
     {
         FastDiv f;
-        f.d = dd;
+        f.d = dd ? dd : 1u;
         uint32_t l = 0;
-        while ((1ull << l) < dd) ++l;
+        while ((1ull << l) < f.d) ++l;
         f.l = l;
-        f.m = (uint32_t)((((1ull << 32) * ((1ull << l) - dd)) / dd) + 1);
+        f.m = (uint32_t)((((1ull << 32) * ((1ull << l) - f.d)) / f.d) + 1);
         return f;
     }
     __device__ __forceinline__ uint32_t div(uint32_t n) const
@@ -29,6 +34,17 @@ struct FastDiv {
         const uint32_t t = __umulhi(m, n);
         return (uint32_t)(((uint64_t)t + n) >> l);
     }
+};
+
+// CPML faces of one axis as the bulk kernels see them: the low ('n') face covers
+// c < Tn, the high ('p') face c >= s - Tp (Tp = 0 when the face never applies). Faces of one
+// axis never overlap in a bulk launch (the plan falls back to the generic kernels then), so
+// every cell sees at most one face per axis and the order of faces cannot change a result.
+template <typename R>
+struct AxisK {
+    int32_t Tn, Tp;
+    const R *n0, *n1, *n2, *p0, *p1, *p2;
+    R *nu, *nv, *pu, *pv;
 };
 
 // One CPML face as one update kernel sees it (E tables for E-type kernels, H tables for
@@ -41,25 +57,29 @@ struct FaceK {
     R *psi_u, *psi_v;
 };
 
-// Arguments of one E-type or H-type launch.
-//   E-type: P += dt/mat * (curl Q + psi)         (update_e.cl:105-107)
-//   H-type: P -= dt[/mat] * (curl Q - psi)       (update_h.cl:129-131)
-// Rp is the other half of Q's complex pair for Bloch boundaries.
+// Arguments of one E-type or H-type update.
+//   E-type: P += dt/eps * (curl Q + psi)         (update_e.cl:105-107)
+//   H-type: P -= dt[/mu] * (curl Q - psi)       (update_h.cl:129-131)
+// coef holds dt/mat precomputed (the same rounded quotient the reference forms per cell);
+// when it is NULL the shell kernels divide. Rp is the other half of Q's complex pair.
 template <typename R>
 struct YeeK {
     R *P;
     const R *Q;
     const R *Rp;
     const R *mat;
+    const R *coef;
     R *oS;
     uint32_t sx, sy, sz, syz;
     uint64_t N;
-    FastDiv dsz;
     R dt, inv_d;
     const R *inv_tab[3];
-    int32_t nface, bloch_mask;
+    int32_t nface, bloch_mask, dxmode, _pad;
     R br[3], bi[3];
     FaceK<R> face[6];
+    AxisK<R> ax[3];
+    FastDiv dsz;
+    int32_t xchunk, bulk;
 };
 
 template <typename R>
@@ -68,8 +88,9 @@ struct SK {
     const R *oS;
     uint32_t sx, sy, sz, syz;
     uint64_t N;
-    FastDiv dsz;
     R sf;
+    FastDiv dsz;
+    int32_t xchunk, _pad;
 };
 
 template <typename R>
@@ -90,5 +111,15 @@ struct PointK {
     const R *values;
     int32_t n, t;
 };
+
+template <typename R>
+struct PrepK {
+    R *out;
+    const R *mat;
+    uint64_t n;
+    R dt;
+};
+
+constexpr int BLOCK = 256;
 
 }  // namespace fdtd

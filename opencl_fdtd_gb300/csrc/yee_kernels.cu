@@ -1,11 +1,18 @@
-// Two-pass Yee kernels behind update_E/H/S/F/G/J (the drop-in path).
+// Yee kernels behind update_E/H/S/F/G/J (the drop-in path).
 //
-// One thread advances one cell (all three components), so each launch covers N threads,
-// where the reference launches 3N work-items and idles two thirds of them
-// (opencl_fdtd/kernels/common.cl:21-25). The grid is (ceil(sy*sz / 256), sx): blockIdx.y is
-// the x plane, so x-face CPML branches are uniform per block, and consecutive threads walk
-// consecutive z, so every field load of a warp is one contiguous 128-byte run. Neighbour
-// re-reads (z-1 and y-1 rows in L1, the x-1 plane in L2) cost no extra HBM traffic.
+// Bulk kernels (the normal path): thread (y, z) of the plane marches a chunk of consecutive
+// x planes. The x-neighbour plane is carried in registers (the E update's x-1 values are the
+// previous iteration's own loads; the H update's x+1 loads become the next iteration's own),
+// and every load of iteration x+1 (fields, neighbours, dt/eps, CPML psi) is issued before
+// iteration x computes and stores, so each warp keeps a full iteration of loads in flight.
+// Consecutive threads walk consecutive z, so a warp's loads are contiguous runs. CPML faces
+// are handled per axis: x-faces are uniform for a whole iteration, y- and z-face membership
+// is fixed for a thread, so the depth index and the coefficients of y/z faces are looked up
+// once per thread. One thread advances all three components of a cell, where the reference
+// launches 3N work-items and idles two thirds of them (opencl_fdtd/kernels/common.cl:21-25).
+//
+// Generic kernels: one thread per cell with the faces applied in list order; used only when
+// two CPML faces of one axis overlap (the order of their terms then matters).
 //
 // This translation unit is compiled with --fmad=false and every expression keeps the
 // reference's operation order, so results match the reference kernel text bit for bit in
@@ -14,6 +21,9 @@
 #include "yee_launch.h"
 
 namespace fdtd {
+
+template <typename T>
+__device__ __forceinline__ T ldg(const T *p) { return __ldg(p); }
 
 // ---- CPML contribution of one face ---------------------------------------------------------
 // Depth index of the cell inside the face's slab, or -1 (update_e.cl:81-90). A 'p' face
@@ -29,32 +39,47 @@ __device__ __forceinline__ int pml_ir(int pol, int T, uint32_t s, uint32_t c)
 // u component (update_e.cl:93-96); both derivatives along r are first scaled by p2 = 1/kappa.
 // E-type kernels fold (psi_u, psi_v) into (P_u, P_v) with signs (-, +) for r in {x, z} and
 // (+, -) for r = y (update_e.cl:73-77, 97-98); H-type kernels use the mirrored signs
-// (update_h.cl:113-114).
+// (update_h.cl:113-114). Returns the new (psi_u, psi_v).
+template <typename R, bool ETYPE, int AX>
+__device__ __forceinline__ void face_update(R p0, R p1, R p2, R su_old, R sv_old, R &su, R &sv,
+                                            R &d_xy, R &d_xz, R &d_yx, R &d_yz, R &d_zx, R &d_zy,
+                                            R &px, R &py, R &pz)
+{
+    R &dv = (AX == 0) ? d_zx : (AX == 1) ? d_zy : d_yz;
+    R &du = (AX == 0) ? d_yx : (AX == 1) ? d_xy : d_xz;
+    dv = dv * p2;
+    du = du * p2;
+    su = p0 * su_old + p1 * dv;
+    sv = p0 * sv_old + p1 * du;
+    R &pu = (AX == 0) ? py : px;
+    R &pv = (AX == 2) ? py : pz;
+    const bool plus_u = ETYPE ? (AX == 1) : (AX != 1);
+    if (plus_u) { pu = pu + su; pv = pv - sv; }
+    else        { pu = pu - su; pv = pv + sv; }
+}
+
+// psi index of cell (x, y, z) at depth ir of a face of axis AX with thickness T
+template <int AX>
+__device__ __forceinline__ uint32_t psi_index(uint32_t ir, uint32_t T, uint32_t x, uint32_t y,
+                                              uint32_t z, uint32_t sy, uint32_t sz)
+{
+    if (AX == 0) return (ir * sy + y) * sz + z;
+    if (AX == 1) return (x * T + ir) * sz + z;
+    return (x * sy + y) * T + ir;
+}
+
 template <typename R, bool ETYPE, int AX>
 __device__ __forceinline__ void pml_face(const FaceK<R> &f, int ir, uint32_t x, uint32_t y,
                                          uint32_t z, uint32_t sy, uint32_t sz,
                                          R &d_xy, R &d_xz, R &d_yx, R &d_yz, R &d_zx, R &d_zy,
                                          R &px, R &py, R &pz)
 {
-    const R p0 = f.p0[ir], p1 = f.p1[ir], p2 = f.p2[ir];
-    uint32_t ip;
-    if (AX == 0) ip = ((uint32_t)ir * sy + y) * sz + z;
-    else if (AX == 1) ip = (x * (uint32_t)f.T + (uint32_t)ir) * sz + z;
-    else ip = (x * sy + y) * (uint32_t)f.T + (uint32_t)ir;
-    // (dv_r, du_r): derivative along AX of the v and the u component
-    R &dv = (AX == 0) ? d_zx : (AX == 1) ? d_zy : d_yz;
-    R &du = (AX == 0) ? d_yx : (AX == 1) ? d_xy : d_xz;
-    dv = dv * p2;
-    du = du * p2;
-    const R su = p0 * f.psi_u[ip] + p1 * dv;
-    const R sv = p0 * f.psi_v[ip] + p1 * du;
+    const uint32_t ip = psi_index<AX>((uint32_t)ir, (uint32_t)f.T, x, y, z, sy, sz);
+    R su, sv;
+    face_update<R, ETYPE, AX>(f.p0[ir], f.p1[ir], f.p2[ir], f.psi_u[ip], f.psi_v[ip], su, sv,
+                              d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
     f.psi_u[ip] = su;
     f.psi_v[ip] = sv;
-    R &pu = (AX == 0) ? py : px;
-    R &pv = (AX == 2) ? py : pz;
-    const bool plus_u = ETYPE ? (AX == 1) : (AX != 1);
-    if (plus_u) { pu = pu + su; pv = pv - sv; }
-    else        { pu = pu - su; pv = pv + sv; }
 }
 
 template <typename R, bool ETYPE>
@@ -82,16 +107,11 @@ __device__ __forceinline__ void pml_all(const YeeK<R> &k, uint32_t x, uint32_t y
     }
 }
 
-// ---- E-type: update_E / update_F (update_e.cl) ---------------------------------------------
+// ---- generic E-type cell: update_E / update_F (update_e.cl) --------------------------------
 template <typename R>
-__global__ void __launch_bounds__(256) k_yee_e(const YeeK<R> k)
+__device__ __forceinline__ void cell_e(const YeeK<R> &k, uint32_t x, uint32_t y, uint32_t z)
 {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= k.syz) return;
-    const uint32_t x = blockIdx.y;
-    const uint32_t y = k.dsz.div(j);
-    const uint32_t z = j - y * k.sz;
-    const uint32_t i = x * k.syz + j;
+    const uint32_t i = (x * k.sy + y) * k.sz + z;
     const uint64_t N = k.N;
     const R *__restrict__ Qx = k.Q;
     const R *__restrict__ Qy = k.Q + N;
@@ -135,22 +155,23 @@ __global__ void __launch_bounds__(256) k_yee_e(const YeeK<R> k)
     if (k.nface) pml_all<R, true>(k, x, y, z, d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
 
     R *Px = k.P, *Py = k.P + N, *Pz = k.P + 2 * N;
-    const R *ex = k.mat, *ey = k.mat + N, *ez = k.mat + 2 * N;
-    Px[i] = Px[i] + (k.dt / ex[i]) * ((d_zy - d_yz) + px);
-    Py[i] = Py[i] + (k.dt / ey[i]) * ((d_xz - d_zx) + py);
-    Pz[i] = Pz[i] + (k.dt / ez[i]) * ((d_yx - d_xy) + pz);
+    R cx, cy, cz;
+    if (k.coef) {
+        cx = k.coef[i]; cy = k.coef[N + i]; cz = k.coef[2 * N + i];
+    } else {
+        cx = k.dt / k.mat[i]; cy = k.dt / k.mat[N + i]; cz = k.dt / k.mat[2 * N + i];
+    }
+    // update_e.cl:105-107
+    Px[i] = Px[i] + cx * ((d_zy - d_yz) + px);
+    Py[i] = Py[i] + cy * ((d_xz - d_zx) + py);
+    Pz[i] = Pz[i] + cz * ((d_yx - d_xy) + pz);
 }
 
-// ---- H-type: update_H / update_G (update_h.cl) ---------------------------------------------
+// ---- generic H-type cell: update_H / update_G (update_h.cl) --------------------------------
 template <typename R, bool MU, bool POYNT>
-__global__ void __launch_bounds__(256) k_yee_h(const YeeK<R> k)
+__device__ __forceinline__ void cell_h(const YeeK<R> &k, uint32_t x, uint32_t y, uint32_t z)
 {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= k.syz) return;
-    const uint32_t x = blockIdx.y;
-    const uint32_t y = k.dsz.div(j);
-    const uint32_t z = j - y * k.sz;
-    const uint32_t i = x * k.syz + j;
+    const uint32_t i = (x * k.sy + y) * k.sz + z;
     const uint64_t N = k.N;
     const R *__restrict__ Qx = k.Q;
     const R *__restrict__ Qy = k.Q + N;
@@ -198,11 +219,17 @@ __global__ void __launch_bounds__(256) k_yee_h(const YeeK<R> k)
     const R ox = Px[i], oy = Py[i], oz = Pz[i];
     R hx, hy, hz;
     if (MU) {
-        const R *mx = k.mat, *my = k.mat + N, *mz = k.mat + 2 * N;
-        hx = ox - (k.dt / mx[i]) * ((d_zy - d_yz) - px);
-        hy = oy - (k.dt / my[i]) * ((d_xz - d_zx) - py);
-        hz = oz - (k.dt / mz[i]) * ((d_yx - d_xy) - pz);
+        R cx, cy, cz;
+        if (k.coef) {
+            cx = k.coef[i]; cy = k.coef[N + i]; cz = k.coef[2 * N + i];
+        } else {
+            cx = k.dt / k.mat[i]; cy = k.dt / k.mat[N + i]; cz = k.dt / k.mat[2 * N + i];
+        }
+        hx = ox - cx * ((d_zy - d_yz) - px);
+        hy = oy - cy * ((d_xz - d_zx) - py);
+        hz = oz - cz * ((d_yx - d_xy) - pz);
     } else {
+        // update_h.cl:129-131
         hx = ox - k.dt * ((d_zy - d_yz) - px);
         hy = oy - k.dt * ((d_xz - d_zx) - py);
         hz = oz - k.dt * ((d_yx - d_xy) - pz);
@@ -211,8 +238,8 @@ __global__ void __launch_bounds__(256) k_yee_h(const YeeK<R> k)
     Py[i] = hy;
     Pz[i] = hz;
     if (POYNT) {
-        // E averaged in space, H in time (update_h.cl:63-70, 135-137), six products
-        // in plane order xy, yz, zx, xz, yx, zy (update_h.cl:142-154)
+        // E averaged in space, H in time (update_h.cl:63-70, 135-137), six products in plane
+        // order xy, yz, zx, xz, yx, zy (update_h.cl:142-154)
         const R ahx = hx + ox, ahy = hy + oy, ahz = hz + oz;
         R *o = k.oS;
         o[0 * N + i] = (r_yx + qy) * ahz;
@@ -224,32 +251,440 @@ __global__ void __launch_bounds__(256) k_yee_h(const YeeK<R> k)
     }
 }
 
+// ---- generic full-grid kernels (overlapping CPML faces) ------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_generic_e(const YeeK<R> k)
+{
+    const uint32_t j = blockIdx.x * BLOCK + threadIdx.x;
+    if (j >= k.syz) return;
+    const uint32_t y = k.dsz.div(j);
+    cell_e<R>(k, blockIdx.y, y, j - y * k.sz);
+}
+
+template <typename R, bool MU, bool POYNT>
+__global__ void __launch_bounds__(BLOCK) k_generic_h(const YeeK<R> k)
+{
+    const uint32_t j = blockIdx.x * BLOCK + threadIdx.x;
+    if (j >= k.syz) return;
+    const uint32_t y = k.dsz.div(j);
+    cell_h<R, MU, POYNT>(k, blockIdx.y, y, j - y * k.sz);
+}
+
+// ---- bulk kernels ----------------------------------------------------------------------------
+// Per-thread view of one axis's CPML faces for a coordinate that stays fixed during the march
+// (y or z): depth index, thickness and coefficients, or ir < 0 outside both faces.
+template <typename R>
+struct FixedFace {
+    int ir;
+    uint32_t T;
+    R p0, p1, p2;
+    R *pu, *pv;
+};
+
+template <typename R, bool ETYPE>
+__device__ __forceinline__ FixedFace<R> fixed_face(const AxisK<R> &a, uint32_t s, uint32_t c)
+{
+    FixedFace<R> f;
+    f.ir = -1;
+    f.T = 0;
+    f.p0 = f.p1 = f.p2 = R(0);
+    f.pu = f.pv = nullptr;
+    if (c < (uint32_t)a.Tn) {
+        f.ir = (int)c;
+        f.T = (uint32_t)a.Tn;
+        f.p0 = ldg(a.n0 + c); f.p1 = ldg(a.n1 + c); f.p2 = ldg(a.n2 + c);
+        f.pu = a.nu;
+        f.pv = a.nv;
+    } else if (a.Tp && c >= s - (uint32_t)a.Tp) {
+        const uint32_t ir = s - 1u - c;
+        f.ir = (int)ir;
+        f.T = (uint32_t)a.Tp;
+        f.p0 = ldg(a.p0 + ir); f.p1 = ldg(a.p1 + ir); f.p2 = ldg(a.p2 + ir);
+        f.pu = a.pu;
+        f.pv = a.pv;
+    }
+    return f;
+}
+
+// x-face of plane x (uniform across the block): depth, thickness and psi arrays
+template <typename R>
+struct XFace {
+    int ir;
+    uint32_t T;
+    const R *t0, *t1, *t2;
+    R *pu, *pv;
+};
+
+template <typename R>
+__device__ __forceinline__ XFace<R> x_face(const AxisK<R> &a, uint32_t sx, uint32_t x)
+{
+    XFace<R> f;
+    f.ir = -1;
+    f.T = 0;
+    f.t0 = f.t1 = f.t2 = nullptr;
+    f.pu = f.pv = nullptr;
+    if (x < (uint32_t)a.Tn) {
+        f.ir = (int)x; f.T = (uint32_t)a.Tn;
+        f.t0 = a.n0; f.t1 = a.n1; f.t2 = a.n2; f.pu = a.nu; f.pv = a.nv;
+    } else if (a.Tp && x >= sx - (uint32_t)a.Tp) {
+        f.ir = (int)(sx - 1u - x); f.T = (uint32_t)a.Tp;
+        f.t0 = a.p0; f.t1 = a.p1; f.t2 = a.p2; f.pu = a.pu; f.pv = a.pv;
+    }
+    return f;
+}
+
+// Values one E-type iteration reads, loaded one iteration ahead.
+template <typename R>
+struct ELoad {
+    R hx, hy, hz;                 // Q at x
+    R nxy, nxz, nyz, nzy;         // Q_x(y-1), Q_x(z-1), Q_y(z-1), Q_z(y-1)
+    R bxy, bzy, bxz, byz;         // Bloch partner at the wrapped y / z neighbour
+    R ex, ey, ez;                 // P at x
+    R cx, cy, cz;                 // dt/eps at x
+    R xu, xv, yu, yv, zu, zv;     // psi of the faces the cell is in
+};
+
+template <typename R, int DX, bool BLOCH>
+__global__ void __launch_bounds__(BLOCK, 3) k_bulk_e(const YeeK<R> k)
+{
+    const uint32_t j = blockIdx.x * BLOCK + threadIdx.x;
+    if (j >= k.syz) return;
+    const uint32_t sx = k.sx, sy = k.sy, sz = k.sz, syz = k.syz;
+    const uint32_t y = k.dsz.div(j);
+    const uint32_t z = j - y * sz;
+    const uint32_t xa = blockIdx.y * (uint32_t)k.xchunk;
+    const uint32_t xb = min(xa + (uint32_t)k.xchunk, sx);
+    const uint64_t N = k.N;
+    const R *__restrict__ Qx = k.Q;
+    const R *__restrict__ Qy = k.Q + N;
+    const R *__restrict__ Qz = k.Q + 2 * N;
+    const R *__restrict__ Cx = k.coef;
+    const R *__restrict__ Cy = k.coef + N;
+    const R *__restrict__ Cz = k.coef + 2 * N;
+    R *__restrict__ Px = k.P;
+    R *__restrict__ Py = k.P + N;
+    R *__restrict__ Pz = k.P + 2 * N;
+    // y/z minus neighbours with periodic wrap (common.cl:75-81), fixed for the thread
+    const uint32_t dmy = y ? 0u - sz : (sy - 1u) * sz;
+    const uint32_t dmz = z ? 0xffffffffu : sz - 1u;
+    const bool by = BLOCH && (k.bloch_mask & 2) && y == 0;
+    const bool bz = BLOCH && (k.bloch_mask & 4) && z == 0;
+    const FixedFace<R> fy = fixed_face<R, true>(k.ax[1], sy, y);
+    const FixedFace<R> fz = fixed_face<R, true>(k.ax[2], sz, z);
+    R iy = k.inv_d, iz = k.inv_d;
+    if (DX == 2) { iy = ldg(k.inv_tab[1] + y); iz = ldg(k.inv_tab[2] + z); }
+
+    auto load = [&](uint32_t x, uint32_t i) {
+        ELoad<R> v;
+        v.hx = ldg(Qx + i); v.hy = ldg(Qy + i); v.hz = ldg(Qz + i);
+        // neighbour indices in 32-bit arithmetic (dmy / dmz may be wrapped negatives)
+        const uint32_t imy = i + dmy, imz = i + dmz;
+        v.nxy = ldg(Qx + imy); v.nxz = ldg(Qx + imz);
+        v.nyz = ldg(Qy + imz); v.nzy = ldg(Qz + imy);
+        v.bxy = v.bzy = v.bxz = v.byz = R(0);
+        if (by) { v.bxy = ldg(k.Rp + imy); v.bzy = ldg(k.Rp + 2 * N + imy); }
+        if (bz) { v.bxz = ldg(k.Rp + imz); v.byz = ldg(k.Rp + N + imz); }
+        v.ex = Px[i]; v.ey = Py[i]; v.ez = Pz[i];
+        v.cx = ldg(Cx + i); v.cy = ldg(Cy + i); v.cz = ldg(Cz + i);
+        v.xu = v.xv = v.yu = v.yv = v.zu = v.zv = R(0);
+        const XFace<R> fx = x_face<R>(k.ax[0], sx, x);
+        if (fx.ir >= 0) {
+            const uint32_t ip = psi_index<0>((uint32_t)fx.ir, fx.T, x, y, z, sy, sz);
+            v.xu = fx.pu[ip]; v.xv = fx.pv[ip];
+        }
+        if (fy.ir >= 0) {
+            const uint32_t ip = psi_index<1>((uint32_t)fy.ir, fy.T, x, y, z, sy, sz);
+            v.yu = fy.pu[ip]; v.yv = fy.pv[ip];
+        }
+        if (fz.ir >= 0) {
+            const uint32_t ip = psi_index<2>((uint32_t)fz.ir, fz.T, x, y, z, sy, sz);
+            v.zu = fz.pu[ip]; v.zv = fz.pv[ip];
+        }
+        return v;
+    };
+
+    uint32_t i = xa * syz + j;
+    // x-1 plane of the first iteration, wrapped and Bloch-coupled at x = 0
+    const uint32_t im = xa ? i - syz : i + (sx - 1u) * syz;
+    R hy_m = ldg(Qy + im), hz_m = ldg(Qz + im);
+    if (BLOCH && xa == 0 && (k.bloch_mask & 1)) {
+        hy_m = hy_m * k.br[0] + ldg(k.Rp + N + im) * k.bi[0];
+        hz_m = hz_m * k.br[0] + ldg(k.Rp + 2 * N + im) * k.bi[0];
+    }
+    ELoad<R> cur = load(xa, i);
+    for (uint32_t x = xa; x < xb; ++x, i += syz) {
+        ELoad<R> nxt;
+        if (x + 1u < xb) nxt = load(x + 1u, i + syz);
+        R n_xy = cur.nxy, n_zy = cur.nzy, n_xz = cur.nxz, n_yz = cur.nyz;
+        if (by) { n_xy = n_xy * k.br[1] + cur.bxy * k.bi[1]; n_zy = n_zy * k.br[1] + cur.bzy * k.bi[1]; }
+        if (bz) { n_xz = n_xz * k.br[2] + cur.bxz * k.bi[2]; n_yz = n_yz * k.br[2] + cur.byz * k.bi[2]; }
+        // backward differences (update_e.cl:39-46)
+        R d_xy = cur.hx - n_xy;
+        R d_xz = cur.hx - n_xz;
+        R d_yx = cur.hy - hy_m;
+        R d_yz = cur.hy - n_yz;
+        R d_zx = cur.hz - hz_m;
+        R d_zy = cur.hz - n_zy;
+        if (DX != 0) {
+            const R ix = (DX == 2) ? ldg(k.inv_tab[0] + x) : k.inv_d;
+            d_xy = d_xy * iy; d_xz = d_xz * iz; d_yx = d_yx * ix;
+            d_yz = d_yz * iz; d_zx = d_zx * ix; d_zy = d_zy * iy;
+        }
+        // CPML (update_e.cl:64-100): at most one face per axis
+        R px = R(0), py = R(0), pz = R(0);
+        const XFace<R> fx = x_face<R>(k.ax[0], sx, x);
+        if (fx.ir >= 0) {
+            R su, sv;
+            face_update<R, true, 0>(ldg(fx.t0 + fx.ir), ldg(fx.t1 + fx.ir), ldg(fx.t2 + fx.ir),
+                                    cur.xu, cur.xv, su, sv, d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
+            const uint32_t ip = psi_index<0>((uint32_t)fx.ir, fx.T, x, y, z, sy, sz);
+            fx.pu[ip] = su; fx.pv[ip] = sv;
+        }
+        if (fy.ir >= 0) {
+            R su, sv;
+            face_update<R, true, 1>(fy.p0, fy.p1, fy.p2, cur.yu, cur.yv, su, sv,
+                                    d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
+            const uint32_t ip = psi_index<1>((uint32_t)fy.ir, fy.T, x, y, z, sy, sz);
+            fy.pu[ip] = su; fy.pv[ip] = sv;
+        }
+        if (fz.ir >= 0) {
+            R su, sv;
+            face_update<R, true, 2>(fz.p0, fz.p1, fz.p2, cur.zu, cur.zv, su, sv,
+                                    d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
+            const uint32_t ip = psi_index<2>((uint32_t)fz.ir, fz.T, x, y, z, sy, sz);
+            fz.pu[ip] = su; fz.pv[ip] = sv;
+        }
+        // update_e.cl:105-107
+        Px[i] = cur.ex + cur.cx * ((d_zy - d_yz) + px);
+        Py[i] = cur.ey + cur.cy * ((d_xz - d_zx) + py);
+        Pz[i] = cur.ez + cur.cz * ((d_yx - d_xy) + pz);
+        hy_m = cur.hy;
+        hz_m = cur.hz;
+        cur = nxt;
+    }
+}
+
+// Values one H-type iteration reads, loaded one iteration ahead.
+template <typename R>
+struct HLoad {
+    R ex1, ey1, ez1;              // Q at x+1 (wrapped)
+    R rxy, rxz, ryz, rzy;         // Q_x(y+1), Q_x(z+1), Q_y(z+1), Q_z(y+1) at x
+    R bxy, bzy, bxz, byz;         // Bloch partner at the wrapped y / z neighbour
+    R byx, bzx;                   // Bloch partner at the wrapped x neighbour
+    R hx, hy, hz;                 // P at x
+    R cx, cy, cz;                 // dt/mu at x
+    R xu, xv, yu, yv, zu, zv;     // psi of the faces the cell is in
+};
+
+template <typename R, int DX, bool MU, bool POYNT, bool BLOCH>
+__global__ void __launch_bounds__(BLOCK, 3) k_bulk_h(const YeeK<R> k)
+{
+    const uint32_t j = blockIdx.x * BLOCK + threadIdx.x;
+    if (j >= k.syz) return;
+    const uint32_t sx = k.sx, sy = k.sy, sz = k.sz, syz = k.syz;
+    const uint32_t y = k.dsz.div(j);
+    const uint32_t z = j - y * sz;
+    const uint32_t xa = blockIdx.y * (uint32_t)k.xchunk;
+    const uint32_t xb = min(xa + (uint32_t)k.xchunk, sx);
+    const uint64_t N = k.N;
+    const R *__restrict__ Qx = k.Q;
+    const R *__restrict__ Qy = k.Q + N;
+    const R *__restrict__ Qz = k.Q + 2 * N;
+    R *__restrict__ Px = k.P;
+    R *__restrict__ Py = k.P + N;
+    R *__restrict__ Pz = k.P + 2 * N;
+    // y/z plus neighbours with periodic wrap (common.cl:82-84), fixed for the thread
+    const uint32_t dpy = (y + 1u < sy) ? sz : 0u - (sy - 1u) * sz;
+    const uint32_t dpz = (z + 1u < sz) ? 1u : 0u - (sz - 1u);
+    const bool bx = BLOCH && (k.bloch_mask & 1) != 0;
+    const bool by = BLOCH && (k.bloch_mask & 2) && y + 1u == sy;
+    const bool bz = BLOCH && (k.bloch_mask & 4) && z + 1u == sz;
+    const FixedFace<R> fy = fixed_face<R, false>(k.ax[1], sy, y);
+    const FixedFace<R> fz = fixed_face<R, false>(k.ax[2], sz, z);
+    R iy = k.inv_d, iz = k.inv_d;
+    if (DX == 2) { iy = ldg(k.inv_tab[1] + y); iz = ldg(k.inv_tab[2] + z); }
+    const R dt = k.dt;
+
+    auto load = [&](uint32_t x, uint32_t i) {
+        HLoad<R> v;
+        const uint32_t i1 = (x + 1u < sx) ? i + syz : i - (sx - 1u) * syz;
+        v.ex1 = ldg(Qx + i1); v.ey1 = ldg(Qy + i1); v.ez1 = ldg(Qz + i1);
+        // neighbour indices in 32-bit arithmetic (dpy / dpz may be wrapped negatives)
+        const uint32_t ipy = i + dpy, ipz = i + dpz;
+        v.rxy = ldg(Qx + ipy); v.rxz = ldg(Qx + ipz);
+        v.ryz = ldg(Qy + ipz); v.rzy = ldg(Qz + ipy);
+        v.bxy = v.bzy = v.bxz = v.byz = v.byx = v.bzx = R(0);
+        if (bx && x + 1u == sx) { v.byx = ldg(k.Rp + N + i1); v.bzx = ldg(k.Rp + 2 * N + i1); }
+        if (by) { v.bxy = ldg(k.Rp + ipy); v.bzy = ldg(k.Rp + 2 * N + ipy); }
+        if (bz) { v.bxz = ldg(k.Rp + ipz); v.byz = ldg(k.Rp + N + ipz); }
+        v.hx = Px[i]; v.hy = Py[i]; v.hz = Pz[i];
+        v.cx = v.cy = v.cz = R(0);
+        if (MU) { v.cx = ldg(k.coef + i); v.cy = ldg(k.coef + N + i); v.cz = ldg(k.coef + 2 * N + i); }
+        v.xu = v.xv = v.yu = v.yv = v.zu = v.zv = R(0);
+        const XFace<R> fx = x_face<R>(k.ax[0], sx, x);
+        if (fx.ir >= 0) {
+            const uint32_t ip = psi_index<0>((uint32_t)fx.ir, fx.T, x, y, z, sy, sz);
+            v.xu = fx.pu[ip]; v.xv = fx.pv[ip];
+        }
+        if (fy.ir >= 0) {
+            const uint32_t ip = psi_index<1>((uint32_t)fy.ir, fy.T, x, y, z, sy, sz);
+            v.yu = fy.pu[ip]; v.yv = fy.pv[ip];
+        }
+        if (fz.ir >= 0) {
+            const uint32_t ip = psi_index<2>((uint32_t)fz.ir, fz.T, x, y, z, sy, sz);
+            v.zu = fz.pu[ip]; v.zv = fz.pv[ip];
+        }
+        return v;
+    };
+
+    uint32_t i = xa * syz + j;
+    R ex = ldg(Qx + i), ey = ldg(Qy + i), ez = ldg(Qz + i);
+    HLoad<R> cur = load(xa, i);
+    for (uint32_t x = xa; x < xb; ++x, i += syz) {
+        HLoad<R> nxt;
+        if (x + 1u < xb) nxt = load(x + 1u, i + syz);
+        R n_yx = cur.ey1, n_zx = cur.ez1, n_xy = cur.rxy, n_zy = cur.rzy, n_xz = cur.rxz, n_yz = cur.ryz;
+        if (bx && x + 1u == sx) { n_yx = n_yx * k.br[0] + cur.byx * k.bi[0]; n_zx = n_zx * k.br[0] + cur.bzx * k.bi[0]; }
+        if (by) { n_xy = n_xy * k.br[1] + cur.bxy * k.bi[1]; n_zy = n_zy * k.br[1] + cur.bzy * k.bi[1]; }
+        if (bz) { n_xz = n_xz * k.br[2] + cur.bxz * k.bi[2]; n_yz = n_yz * k.br[2] + cur.byz * k.bi[2]; }
+        // forward differences (update_h.cl:36-43)
+        R d_xy = n_xy - ex;
+        R d_xz = n_xz - ex;
+        R d_yx = n_yx - ey;
+        R d_yz = n_yz - ey;
+        R d_zx = n_zx - ez;
+        R d_zy = n_zy - ez;
+        if (DX != 0) {
+            const R ix = (DX == 2) ? ldg(k.inv_tab[0] + x) : k.inv_d;
+            d_xy = d_xy * iy; d_xz = d_xz * iz; d_yx = d_yx * ix;
+            d_yz = d_yz * iz; d_zx = d_zx * ix; d_zy = d_zy * iy;
+        }
+        // CPML (update_h.cl:80-116): at most one face per axis
+        R px = R(0), py = R(0), pz = R(0);
+        const XFace<R> fx = x_face<R>(k.ax[0], sx, x);
+        if (fx.ir >= 0) {
+            R su, sv;
+            face_update<R, false, 0>(ldg(fx.t0 + fx.ir), ldg(fx.t1 + fx.ir), ldg(fx.t2 + fx.ir),
+                                     cur.xu, cur.xv, su, sv, d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
+            const uint32_t ip = psi_index<0>((uint32_t)fx.ir, fx.T, x, y, z, sy, sz);
+            fx.pu[ip] = su; fx.pv[ip] = sv;
+        }
+        if (fy.ir >= 0) {
+            R su, sv;
+            face_update<R, false, 1>(fy.p0, fy.p1, fy.p2, cur.yu, cur.yv, su, sv,
+                                     d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
+            const uint32_t ip = psi_index<1>((uint32_t)fy.ir, fy.T, x, y, z, sy, sz);
+            fy.pu[ip] = su; fy.pv[ip] = sv;
+        }
+        if (fz.ir >= 0) {
+            R su, sv;
+            face_update<R, false, 2>(fz.p0, fz.p1, fz.p2, cur.zu, cur.zv, su, sv,
+                                     d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
+            const uint32_t ip = psi_index<2>((uint32_t)fz.ir, fz.T, x, y, z, sy, sz);
+            fz.pu[ip] = su; fz.pv[ip] = sv;
+        }
+        R hx, hy, hz;
+        if (MU) {
+            hx = cur.hx - cur.cx * ((d_zy - d_yz) - px);
+            hy = cur.hy - cur.cy * ((d_xz - d_zx) - py);
+            hz = cur.hz - cur.cz * ((d_yx - d_xy) - pz);
+        } else {
+            // update_h.cl:129-131
+            hx = cur.hx - dt * ((d_zy - d_yz) - px);
+            hy = cur.hy - dt * ((d_xz - d_zx) - py);
+            hz = cur.hz - dt * ((d_yx - d_xy) - pz);
+        }
+        Px[i] = hx;
+        Py[i] = hy;
+        Pz[i] = hz;
+        if (POYNT) {
+            // E averaged in space with the plain wrapped neighbours, H in time
+            // (update_h.cl:63-70, 135-137); planes xy, yz, zx, xz, yx, zy (update_h.cl:142-154)
+            const R ahx = hx + cur.hx, ahy = hy + cur.hy, ahz = hz + cur.hz;
+            R *o = k.oS;
+            o[0 * N + i] = (cur.ey1 + ey) * ahz;
+            o[3 * N + i] = (-(cur.ez1 + ez)) * ahy;
+            o[1 * N + i] = (cur.rzy + ez) * ahx;
+            o[4 * N + i] = (-(cur.rxy + ex)) * ahz;
+            o[2 * N + i] = (cur.rxz + ex) * ahy;
+            o[5 * N + i] = (-(cur.ryz + ey)) * ahx;
+        }
+        ex = cur.ex1;
+        ey = cur.ey1;
+        ez = cur.ez1;
+        cur = nxt;
+    }
+}
+
 // ---- update_S (update_s.cl:33-36) ----------------------------------------------------------
 template <typename R>
-__global__ void __launch_bounds__(256) k_poynting(const SK<R> k)
+struct SLoad {
+    R xy, yz, zx, xz, yx, zy;     // oS planes at x
+    R xy_y, xz_z, yz_z, zy_y;     // oS_xy(y-1), oS_xz(z-1), oS_yz(z-1), oS_zy(y-1)
+};
+
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_bulk_s(const SK<R> k)
 {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t j = blockIdx.x * BLOCK + threadIdx.x;
     if (j >= k.syz) return;
-    const uint32_t x = blockIdx.y;
+    const uint32_t sx = k.sx, sy = k.sy, sz = k.sz, syz = k.syz;
     const uint32_t y = k.dsz.div(j);
-    const uint32_t z = j - y * k.sz;
-    const uint32_t i = x * k.syz + j;
+    const uint32_t z = j - y * sz;
+    const uint32_t xa = blockIdx.y * (uint32_t)k.xchunk;
+    const uint32_t xb = min(xa + (uint32_t)k.xchunk, sx);
     const uint64_t N = k.N;
-    const uint32_t imx = x ? i - k.syz : i + (k.sx - 1u) * k.syz;
-    const uint32_t imy = y ? i - k.sz : i + (k.sy - 1u) * k.sz;
-    const uint32_t imz = z ? i - 1u : i + (k.sz - 1u);
-    const R *oxy = k.oS, *oyz = k.oS + N, *ozx = k.oS + 2 * N;
-    const R *oxz = k.oS + 3 * N, *oyx = k.oS + 4 * N, *ozy = k.oS + 5 * N;
-    k.S[i] = (((oxy[i] + oxz[i]) + oxy[imy]) + oxz[imz]) * k.sf;
-    k.S[N + i] = (((oyz[i] + oyx[i]) + oyz[imz]) + oyx[imx]) * k.sf;
-    k.S[2 * N + i] = (((ozx[i] + ozy[i]) + ozx[imx]) + ozy[imy]) * k.sf;
+    const R *__restrict__ oxy = k.oS;
+    const R *__restrict__ oyz = k.oS + N;
+    const R *__restrict__ ozx = k.oS + 2 * N;
+    const R *__restrict__ oxz = k.oS + 3 * N;
+    const R *__restrict__ oyx = k.oS + 4 * N;
+    const R *__restrict__ ozy = k.oS + 5 * N;
+    R *__restrict__ Sx = k.S;
+    R *__restrict__ Sy = k.S + N;
+    R *__restrict__ Sz = k.S + 2 * N;
+    const uint32_t dmy = y ? 0u - sz : (sy - 1u) * sz;
+    const uint32_t dmz = z ? 0xffffffffu : sz - 1u;
+    auto load = [&](uint32_t i) {
+        SLoad<R> v;
+        v.xy = ldg(oxy + i); v.yz = ldg(oyz + i); v.zx = ldg(ozx + i);
+        v.xz = ldg(oxz + i); v.yx = ldg(oyx + i); v.zy = ldg(ozy + i);
+        const uint32_t imy = i + dmy, imz = i + dmz;   // 32-bit wrap arithmetic
+        v.xy_y = ldg(oxy + imy); v.xz_z = ldg(oxz + imz);
+        v.yz_z = ldg(oyz + imz); v.zy_y = ldg(ozy + imy);
+        return v;
+    };
+    uint32_t i = xa * syz + j;
+    const uint32_t im = xa ? i - syz : i + (sx - 1u) * syz;
+    R yx_m = ldg(oyx + im), zx_m = ldg(ozx + im);
+    const R sf = k.sf;
+    SLoad<R> cur = load(i);
+    for (uint32_t x = xa; x < xb; ++x, i += syz) {
+        SLoad<R> nxt;
+        if (x + 1u < xb) nxt = load(i + syz);
+        Sx[i] = (((cur.xy + cur.xz) + cur.xy_y) + cur.xz_z) * sf;
+        Sy[i] = (((cur.yz + cur.yx) + cur.yz_z) + yx_m) * sf;
+        Sz[i] = (((cur.zx + cur.zy) + zx_m) + cur.zy_y) * sf;
+        yx_m = cur.yx;
+        zx_m = cur.zx;
+        cur = nxt;
+    }
+}
+
+// ---- dt / material coefficients (the quotient update_e.cl:105-107 forms per cell) ----------
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_prepare(const PrepK<R> k)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; i < k.n;
+         i += (uint64_t)gridDim.x * BLOCK)
+        k.out[i] = k.dt / k.mat[i];
 }
 
 // ---- update_J (update_j.cl:23-32), launched over the box only -------------------------------
 template <typename R>
-__global__ void __launch_bounds__(256) k_fieldsrc(const JK<R> k)
+__global__ void __launch_bounds__(BLOCK) k_fieldsrc(const JK<R> k)
 {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t t = blockIdx.x * BLOCK + threadIdx.x;
     const uint32_t nbox = k.nx * k.ny * k.nz;
     if (t >= nbox) return;
     const uint32_t bx = k.dnyz.div(t);
@@ -275,36 +710,90 @@ __global__ void k_point_sources(const PointK<R> k)
 }
 
 // ---- launchers ------------------------------------------------------------------------------
+static inline dim3 bulk_grid(uint32_t syz, uint32_t sx, int xchunk)
+{
+    return dim3((syz + BLOCK - 1) / BLOCK, (sx + (uint32_t)xchunk - 1) / (uint32_t)xchunk, 1);
+}
+
 static inline dim3 plane_grid(uint32_t syz, uint32_t sx)
 {
-    return dim3((syz + 255u) / 256u, sx, 1);
+    return dim3((syz + BLOCK - 1) / BLOCK, sx, 1);
 }
 
 template <typename R>
 cudaError_t launch_yee_e(const YeeK<R> &k, cudaStream_t st)
 {
-    k_yee_e<R><<<plane_grid(k.syz, k.sx), 256, 0, st>>>(k);
+    if (!k.bulk) {
+        k_generic_e<R><<<plane_grid(k.syz, k.sx), BLOCK, 0, st>>>(k);
+        return cudaGetLastError();
+    }
+    const dim3 g = bulk_grid(k.syz, k.sx, k.xchunk);
+    if (k.bloch_mask) {
+        if (k.dxmode == 0) k_bulk_e<R, 0, true><<<g, BLOCK, 0, st>>>(k);
+        else if (k.dxmode == 1) k_bulk_e<R, 1, true><<<g, BLOCK, 0, st>>>(k);
+        else k_bulk_e<R, 2, true><<<g, BLOCK, 0, st>>>(k);
+    } else {
+        if (k.dxmode == 0) k_bulk_e<R, 0, false><<<g, BLOCK, 0, st>>>(k);
+        else if (k.dxmode == 1) k_bulk_e<R, 1, false><<<g, BLOCK, 0, st>>>(k);
+        else k_bulk_e<R, 2, false><<<g, BLOCK, 0, st>>>(k);
+    }
     return cudaGetLastError();
+}
+
+template <typename R, int DX, bool BLOCH>
+static void bulk_h(const YeeK<R> &k, bool mu, bool poynting, cudaStream_t st)
+{
+    const dim3 g = bulk_grid(k.syz, k.sx, k.xchunk);
+    if (mu) {
+        if (poynting) k_bulk_h<R, DX, true, true, BLOCH><<<g, BLOCK, 0, st>>>(k);
+        else k_bulk_h<R, DX, true, false, BLOCH><<<g, BLOCK, 0, st>>>(k);
+    } else {
+        if (poynting) k_bulk_h<R, DX, false, true, BLOCH><<<g, BLOCK, 0, st>>>(k);
+        else k_bulk_h<R, DX, false, false, BLOCH><<<g, BLOCK, 0, st>>>(k);
+    }
+}
+
+template <typename R, int DX>
+static void bulk_h_dispatch(const YeeK<R> &k, bool mu, bool poynting, cudaStream_t st)
+{
+    if (k.bloch_mask) bulk_h<R, DX, true>(k, mu, poynting, st);
+    else bulk_h<R, DX, false>(k, mu, poynting, st);
 }
 
 template <typename R>
 cudaError_t launch_yee_h(const YeeK<R> &k, bool mu, bool poynting, cudaStream_t st)
 {
-    const dim3 g = plane_grid(k.syz, k.sx);
-    if (mu) {
-        if (poynting) k_yee_h<R, true, true><<<g, 256, 0, st>>>(k);
-        else k_yee_h<R, true, false><<<g, 256, 0, st>>>(k);
-    } else {
-        if (poynting) k_yee_h<R, false, true><<<g, 256, 0, st>>>(k);
-        else k_yee_h<R, false, false><<<g, 256, 0, st>>>(k);
+    if (!k.bulk) {
+        const dim3 g = plane_grid(k.syz, k.sx);
+        if (mu) {
+            if (poynting) k_generic_h<R, true, true><<<g, BLOCK, 0, st>>>(k);
+            else k_generic_h<R, true, false><<<g, BLOCK, 0, st>>>(k);
+        } else {
+            if (poynting) k_generic_h<R, false, true><<<g, BLOCK, 0, st>>>(k);
+            else k_generic_h<R, false, false><<<g, BLOCK, 0, st>>>(k);
+        }
+        return cudaGetLastError();
     }
+    if (k.dxmode == 0) bulk_h_dispatch<R, 0>(k, mu, poynting, st);
+    else if (k.dxmode == 1) bulk_h_dispatch<R, 1>(k, mu, poynting, st);
+    else bulk_h_dispatch<R, 2>(k, mu, poynting, st);
     return cudaGetLastError();
 }
 
 template <typename R>
 cudaError_t launch_poynting(const SK<R> &k, cudaStream_t st)
 {
-    k_poynting<R><<<plane_grid(k.syz, k.sx), 256, 0, st>>>(k);
+    k_bulk_s<R><<<bulk_grid(k.syz, k.sx, k.xchunk), BLOCK, 0, st>>>(k);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_prepare(const PrepK<R> &k, cudaStream_t st)
+{
+    if (k.n == 0) return cudaSuccess;
+    const uint64_t want = (k.n + BLOCK - 1) / BLOCK;
+    const unsigned g = (unsigned)(want < 65535ull * 16 ? want : 65535ull * 16);
+    k_prepare<R><<<g, BLOCK, 0, st>>>(k);
     return cudaGetLastError();
 }
 
@@ -313,7 +802,7 @@ cudaError_t launch_fieldsrc(const JK<R> &k, cudaStream_t st)
 {
     const uint32_t n = k.nx * k.ny * k.nz;
     if (n == 0) return cudaSuccess;
-    k_fieldsrc<R><<<(n + 255u) / 256u, 256, 0, st>>>(k);
+    k_fieldsrc<R><<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(k);
     return cudaGetLastError();
 }
 
@@ -329,6 +818,7 @@ cudaError_t launch_point_sources(const PointK<R> &k, cudaStream_t st)
     template cudaError_t launch_yee_e<R>(const YeeK<R> &, cudaStream_t);               \
     template cudaError_t launch_yee_h<R>(const YeeK<R> &, bool, bool, cudaStream_t);   \
     template cudaError_t launch_poynting<R>(const SK<R> &, cudaStream_t);              \
+    template cudaError_t launch_prepare<R>(const PrepK<R> &, cudaStream_t);            \
     template cudaError_t launch_fieldsrc<R>(const JK<R> &, cudaStream_t);              \
     template cudaError_t launch_point_sources<R>(const PointK<R> &, cudaStream_t);
 

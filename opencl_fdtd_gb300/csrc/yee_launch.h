@@ -8,6 +8,7 @@ namespace fdtd {
 template <typename R> cudaError_t launch_yee_e(const YeeK<R> &k, cudaStream_t st);
 template <typename R> cudaError_t launch_yee_h(const YeeK<R> &k, bool mu, bool poynting, cudaStream_t st);
 template <typename R> cudaError_t launch_poynting(const SK<R> &k, cudaStream_t st);
+template <typename R> cudaError_t launch_prepare(const PrepK<R> &k, cudaStream_t st);
 template <typename R> cudaError_t launch_fieldsrc(const JK<R> &k, cudaStream_t st);
 template <typename R> cudaError_t launch_point_sources(const PointK<R> &k, cudaStream_t st);
 

@@ -194,6 +194,11 @@ class Simulation:
 
         self._create_pmls(pmls)
         self._create_plan(uniform_dx)
+        # dt/eps and dt/mu, the per-cell quotients of the updates, cached on the device and
+        # refreshed whenever eps or mu change (tracked through torch's version counter)
+        self._ce = torch.empty_like(self.eps)
+        self._cm = torch.empty_like(self.mu) if self.mu is not None else None
+        self._mat_key = None
         self._buf_key = None
         self._buf = _lib.FdtdBuffers()
         self.steps_run = 0
@@ -338,10 +343,19 @@ class Simulation:
             raise ValueError("{} must be a contiguous {} tensor of {} elements on {}".format(
                 name, self._dtype, numel, self.device))
 
+    def refresh_materials(self):
+        """Recompute the cached dt/eps and dt/mu; needed only after eps or mu were changed
+        by something other than a torch operation (torch in-place ops are detected)."""
+        self._mat_key = None
+        self._buffers()
+
     def _buffers(self) -> _lib.FdtdBuffers:
         key = (id(self.E), id(self.H), id(self.F), id(self.G), id(self.S), id(self.oS),
                id(self.eps), id(self.mu), id(self.Jr), id(self.Ji))
         if key == self._buf_key:
+            mk = (self.eps._version, None if self.mu is None else self.mu._version)
+            if mk != self._mat_key:
+                self._prepare(mk)
             return self._buf
         n3 = 3 * self.N
         b = _lib.FdtdBuffers()
@@ -370,9 +384,18 @@ class Simulation:
             for r in range(3):
                 b.inv_de[r] = self.inv_dxes[r].data_ptr()
                 b.inv_dh[r] = self.inv_dxes[3 + r].data_ptr()
+        b.ce = self._ce.data_ptr()
+        if self._cm is not None:
+            b.cm = self._cm.data_ptr()
         self._buf = b
         self._buf_key = key
+        self._prepare((self.eps._version, None if self.mu is None else self.mu._version))
         return b
+
+    def _prepare(self, mat_key):
+        _lib.check(self._lib.fdtd_prepare(self._plan, ctypes.byref(self._buf),
+                                          ctypes.c_void_p(self.queue.cuda_stream)))
+        self._mat_key = mat_key
 
     def _stream_handle(self, wait_for):
         stream = self.queue
