@@ -55,6 +55,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--xchunk", type=int, default=0, help="x planes per thread (0: plan default)")
+    ap.add_argument("--fused-cells", type=int, default=0)
+    ap.add_argument("--fused-xchunk", type=int, default=0)
+    ap.add_argument("--slab", type=int, default=-1, help="x planes per L2 slab (-1: plan default)")
+    ap.add_argument("--path", choices=["fused", "slab", "dropin", "all"], default="all",
+                    help="slab = Simulation.run over the per-update kernels (whole grid by default)")
     return ap.parse_args()
 
 
@@ -209,34 +214,12 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
-def main():
-    args = parse()
-    if args.impl == "reference":
-        run_reference(args)
-        return
+def time_dropin(sim, lib, wave_dev, ind, K, W, poynting, world):
+    """K per-call steps (update_E, source add, update_H, update_S) with CUDA events around
+    every launch; returns total and per-kernel milliseconds."""
     import torch
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    from opencl_fdtd_gb300 import Simulation, workloads, _lib
-
-    wl = workloads.get(args.workload)
-    kw = wl["kwargs"]
-    sim = Simulation(**kw)
-    if args.xchunk:
-        _lib.check(sim._lib.fdtd_plan_tune(sim._plan, args.xchunk))
-    N = int(numpy.prod(wl["shape"]))
-    fc = workloads.face_cells(wl["shape"], kw["pmls"])
-    poynting = kw.get("do_poynting", True)
-    elem = 4 if kw.get("float_type", numpy.float32) == numpy.float32 else 8
-    K, W = args.steps, args.warmup
-    ind = wl["source_index"]
+    from opencl_fdtd_gb300 import _lib
     stream = sim.queue
-    waves = numpy.array([wl["wave"](t) for t in range(W + K)], dtype=numpy.float32)
-    wave_dev = torch.from_numpy(waves).cuda()
-    lib = sim._lib
     plan = sim._plan
     bufp = ctypes.byref(sim._buffers())
     st = ctypes.c_void_p(stream.cuda_stream)
@@ -266,48 +249,151 @@ def main():
         if world > 1:
             torch.distributed.barrier()
         evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(K)]
-        clocks = ClockSampler(local)
-        clocks.start()
-        time.sleep(0.3)
         torch.cuda.synchronize()
         for t in range(K):
             step(W + t, evs[t])
         torch.cuda.synchronize()
-        clock = clocks.stop()
         if world > 1:
             torch.distributed.barrier()
-    total_ms = evs[0][0].elapsed_time(evs[-1][4])
-    ke = [evs[t][0].elapsed_time(evs[t][1]) for t in range(K)]
-    kh = [evs[t][2].elapsed_time(evs[t][3]) for t in range(K)]
-    ks = [evs[t][3].elapsed_time(evs[t][4]) for t in range(K)]
-    if world > 1:
-        tt = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(tt.item())
-    ms_per_step = total_ms / K
-    value = world * N * K / (total_ms * 1e-3) / 1e6
-
-    per_launch, step_bytes = algorithmic_bytes(N, fc, elem, poynting)
-    means = {"k_yee_e": statistics.mean(ke), "k_yee_h": statistics.mean(kh)}
+    total = evs[0][0].elapsed_time(evs[-1][4])
+    per = {"k_yee_e": statistics.mean(evs[t][0].elapsed_time(evs[t][1]) for t in range(K)),
+           "k_yee_h": statistics.mean(evs[t][2].elapsed_time(evs[t][3]) for t in range(K))}
     if poynting:
-        means["k_poynting"] = statistics.mean(ks)
-    dom = max(means, key=lambda k: means[k])
+        per["k_poynting"] = statistics.mean(evs[t][3].elapsed_time(evs[t][4]) for t in range(K))
+    return total, per
+
+
+def time_run(sim, lib, wave_dev, ind, K, W, world, fused: bool):
+    """K steps in one fdtd_run call bracketed by CUDA events: fused (one kernel per step,
+    scratch buffers attached) or the per-update kernels over L2-resident slabs."""
+    import torch
+    from opencl_fdtd_gb300 import _lib
+    stream = sim.queue
+    if fused:
+        sim._ensure_scratch()
+    bufs = sim._buffers()
+    sim._attach_scratch(fused)
+    st = ctypes.c_void_p(stream.cuda_stream)
+    idx = (ctypes.c_int64 * 1)(ind)
+    esz = wave_dev.element_size()
+    warm = _lib.FdtdPointSources(1, 0, ctypes.addressof(idx), wave_dev.data_ptr())
+    timed = _lib.FdtdPointSources(1, 0, ctypes.addressof(idx), wave_dev.data_ptr() + W * esz)
+    with torch.cuda.stream(stream):
+        _lib.check(lib.fdtd_run(sim._plan, ctypes.byref(bufs), st, W, ctypes.byref(warm)))
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _lib.check(lib.fdtd_run(sim._plan, ctypes.byref(bufs), st, K, ctypes.byref(timed)))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+    return e0.elapsed_time(e1)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from opencl_fdtd_gb300 import Simulation, workloads
+
+    wl = workloads.get(args.workload)
+    kw = wl["kwargs"]
+    sim = Simulation(**kw)
+    if args.xchunk:
+        sim.tune(xchunk=args.xchunk)
+    if args.fused_cells:
+        sim.tune(fused_cells=args.fused_cells)
+    if args.fused_xchunk:
+        sim.tune(fused_xchunk=args.fused_xchunk)
+    if args.slab >= 0:
+        sim.tune(slab=args.slab)
+    N = int(numpy.prod(wl["shape"]))
+    fc = workloads.face_cells(wl["shape"], kw["pmls"])
+    poynting = kw.get("do_poynting", True)
+    elem = 4 if kw.get("float_type", numpy.float32) == numpy.float32 else 8
+    K, W = args.steps, args.warmup
+    ind = wl["source_index"]
+    waves = numpy.array([wl["wave"](t) for t in range(W + K)], dtype=numpy.float32)
+    wave_dev = torch.from_numpy(waves).cuda()
+    lib = sim._lib
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    res = {}
+    if args.path in ("dropin", "all"):
+        res["dropin"] = time_dropin(sim, lib, wave_dev, ind, K, W, poynting, world)
+    if args.path in ("slab", "all"):
+        res["slab"] = time_run(sim, lib, wave_dev, ind, K, W, world, fused=False)
+        sim.tune(slab=0)
+    if args.path in ("fused", "all"):
+        res["fused"] = time_run(sim, lib, wave_dev, ind, K, W, world, fused=True)
+    clock = clocks.stop()
+
+    def allmax(v):
+        if world == 1:
+            return v
+        tt = torch.tensor([v], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        return float(tt.item())
+
     peak, peak_kind = peak_hbm()
-    achieved = per_launch[dom] / (means[dom] * 1e-3) / 1e9
-    traffic = committed_traffic(args.workload).get(dom)
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
-                "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "traffic": traffic, "algorithmic_bytes_per_launch": per_launch[dom],
-                "mean_launch_ms": round(means[dom], 5),
-                "per_kernel_ms": {k: round(v, 5) for k, v in means.items()}}
-    step_gbs = step_bytes / (ms_per_step * 1e-3) / 1e9
-    step_roof = {"achieved": round(step_gbs, 1), "peak": peak, "unit": "GB/s",
-                 "frac": round(step_gbs / peak, 4), "bytes_per_step": step_bytes,
-                 "accounting": "84 B/cell E+H, +12 B/cell S, +32 B per CPML face-cell (f32)"}
+    per_launch, step_bytes = algorithmic_bytes(N, fc, elem, poynting)
+    traffic = committed_traffic(args.workload)
+    out_paths = {}
+    if "dropin" in res:
+        total, per = res["dropin"]
+        total = allmax(total)
+        dom = max(per, key=lambda k: per[k])
+        ach = per_launch[dom] / (per[dom] * 1e-3) / 1e9
+        out_paths["dropin"] = {
+            "ms_per_step": total / K, "value": world * N * K / (total * 1e-3) / 1e6,
+            "gpu_launches": (3 if poynting else 2) * K,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(ach / peak, 4), "peak_source": peak_kind,
+                         "traffic": traffic.get(dom), "algorithmic_bytes_per_launch": per_launch[dom],
+                         "mean_launch_ms": round(per[dom], 5),
+                         "per_kernel_ms": {k: round(v, 5) for k, v in per.items()}}}
+    compulsory = N * (18 if poynting else 15) * elem + fc * 8 * elem
+    for name in ("fused", "slab"):
+        if name not in res:
+            continue
+        total = allmax(res[name])
+        ms = total / K
+        ach = step_bytes / (ms * 1e-3) / 1e9
+        nslab = (wl["shape"][0] + sim.slab_planes() - 1) // sim.slab_planes()
+        launches = K if name == "fused" else K * ((3 if poynting else 2) * nslab + (3 if poynting else 1) + 1)
+        out_paths[name] = {
+            "ms_per_step": ms, "value": world * N * K / (total * 1e-3) / 1e6, "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": "k_fused_step" if name == "fused" else "step (k_bulk_e/h/s over L2 slabs)",
+                         "achieved": round(ach, 1),
+                         "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4),
+                         "peak_source": peak_kind, "traffic": traffic.get(name),
+                         "algorithmic_bytes_per_launch" if name == "fused" else "algorithmic_bytes_per_step": step_bytes,
+                         "accounting": "84 B/cell E+H, +12 B/cell S, +32 B per CPML face-cell (f32)",
+                         "compulsory_bytes_per_step": compulsory,
+                         "compulsory_frac": round(compulsory / (ms * 1e-3) / 1e9 / peak, 4),
+                         "mean_step_ms": round(ms, 5)}}
+    cands = [n for n in ("fused", "slab") if n in out_paths]
+    head = min(cands, key=lambda n: out_paths[n]["ms_per_step"]) if cands else "dropin"
+    hp = out_paths[head]
+    step_gbs = step_bytes / (hp["ms_per_step"] * 1e-3) / 1e9
 
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(sim, wl, args.e2e_steps, world)
+        e2e = run_e2e(sim, wl, args.e2e_steps, world, run_api=(head != "dropin"),
+                      fused=(head == "fused"))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -315,28 +401,61 @@ def main():
 
     if rank == 0:
         out = {
-            "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
-            "steps": K, "warmup": W, "ms_per_step": round(ms_per_step, 5),
+            "metric": METRIC, "value": round(hp["value"], 2), "unit": UNIT, "n_gpus": world,
+            "steps": K, "warmup": W, "ms_per_step": round(hp["ms_per_step"], 5),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded L3 cavity geometry and source)",
             "config": {"workload": wl["describe"], "grid": list(wl["shape"]), "cells": N,
-                       "cpml_face_cells": fc, "path": "drop-in update_E/H/S (two-pass + S pass)",
+                       "cpml_face_cells": fc,
+                       "path": {"fused": "Simulation.run: one fused E+source+H+S kernel per step",
+                                "slab": "Simulation.run: update kernels over L2-resident x slabs",
+                                "dropin": "per-call update_E / source add / update_H / update_S"}[head],
                        "l2": "inputs (~%.0f MB of fields) larger than the 129 MB L2; no flush"
                              % (sim.E.numel() * elem * (6 if poynting else 3) / 1e6),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "roofline": roofline, "step_roofline": step_roof, "clocks": clock,
-            "e2e": e2e, "gpu_launches": (3 if poynting else 2) * K,
+            "roofline": hp["roofline"],
+            "step_roofline": {"achieved": round(step_gbs, 1), "peak": peak, "unit": "GB/s",
+                              "frac": round(step_gbs / peak, 4), "bytes_per_step": step_bytes},
+            "clocks": clock, "e2e": e2e, "gpu_launches": hp["gpu_launches"],
             "cpu_baseline": cpu,
+            "paths": {k: {"value": round(v["value"], 2), "ms_per_step": round(v["ms_per_step"], 5),
+                          "roofline_frac": v["roofline"]["frac"], "kernel": v["roofline"]["kernel"]}
+                      for k, v in out_paths.items()},
         }
+        if "dropin" in out_paths:
+            out["dropin_roofline"] = out_paths["dropin"]["roofline"]
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
-def run_e2e(sim, wl, steps: int, world: int):
-    """The public API loop of fdtd.py:162-175 with the source sample copied from pinned host
-    memory each step and the driven field component read back into pinned memory."""
+def run_e2e(sim, wl, steps: int, world: int, run_api: bool = False, fused: bool = False):
+    """End to end through the public API with host buffers.
+
+    fused: Simulation.run() in calls of 10 steps, each given its 10 source samples from host
+    memory (copied to the device inside the call) and followed by a device-to-host read of
+    the driven field sample. Otherwise the per-call loop of fdtd.py:162-175 with the source
+    sample copied from pinned host memory each step and the field sample read back."""
     import torch
+    if run_api:
+        ind = wl["source_index"]
+        chunk = 10
+        host = numpy.array([wl["wave"](t) for t in range(steps + 2 * chunk)], dtype=numpy.float64)
+        probe = numpy.empty(steps // chunk + 2, numpy.float32)
+        sim.run(chunk, point_sources=[(ind, host[:chunk])], fused=fused).wait()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        n = 0
+        for c in range(steps // chunk):
+            sim.run(chunk, point_sources=[(ind, host[c * chunk:(c + 1) * chunk])], fused=fused)
+            probe[c] = float(sim.E[ind:ind + 1].cpu())
+            n += chunk
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        N = int(numpy.prod(wl["shape"]))
+        return {"value": round(world * N * n / el / 1e6, 2), "unit": UNIT,
+                "h2d_bytes_per_step": 4, "d2h_bytes_per_step": round(4 / chunk, 2), "steps": n,
+                "api": "Simulation.run(10 steps, point_sources from host) + field sample read back"}
     ind = wl["source_index"]
     poynting = wl["kwargs"].get("do_poynting", True)
     host_src = torch.from_numpy(numpy.array([wl["wave"](t) for t in range(steps)],

@@ -95,6 +95,13 @@ typedef struct FdtdBuffers {
      * filled by fdtd_prepare. When set they must be current; when NULL every cell divides,
      * which is slower but gives the same result. */
     void *ce, *cm;
+    /* Optional scratch of the fused multi-step path of fdtd_run: second copies of E, H and
+     * of every psi_e / psi_h array (same sizes). When all are set, fdtd_run advances each
+     * step with one fused kernel that reads one copy and writes the other; at the end the
+     * result is always back in E, H, psi_e, psi_h. When NULL, fdtd_run uses the per-update
+     * kernels. Results are identical either way. */
+    void *E2, *H2;
+    void *psi_e2[6][2], *psi_h2[6][2];
 } FdtdBuffers;
 
 typedef struct FdtdPlan FdtdPlan;
@@ -110,9 +117,19 @@ const char *fdtd_last_error(void);
 int fdtd_plan_create(const FdtdDesc *desc, FdtdPlan **out);
 int fdtd_plan_destroy(FdtdPlan *plan);
 
-/* Tuning: number of consecutive x planes one thread of the update kernels advances
- * (default 16). Any value gives the same results. */
-int fdtd_plan_tune(FdtdPlan *plan, int32_t xchunk);
+/* Tuning keys of fdtd_plan_tune. Any values give the same results.
+ *   XCHUNK        consecutive x planes one thread of the update kernels advances (default 8)
+ *   SLAB          x planes per L2-resident slab of fdtd_run's per-update schedule
+ *                 (default 0 = whole grid)
+ *   FUSED_CELLS   plane cells one block of the fused step owns (0 = the maximum, 768 - 2*sz)
+ *   FUSED_XCHUNK  x planes one block of the fused step marches (default 16) */
+#define FDTD_TUNE_XCHUNK 1
+#define FDTD_TUNE_SLAB 2
+#define FDTD_TUNE_FUSED_CELLS 3
+#define FDTD_TUNE_FUSED_XCHUNK 4
+int fdtd_plan_tune(FdtdPlan *plan, int32_t key, int32_t value);
+/* Current value of a tuning key. */
+int fdtd_plan_get(const FdtdPlan *plan, int32_t key, int32_t *value);
 
 /* Fill buf->ce = dt/eps and, with has_mu, buf->cm = dt/mu (IEEE division, the quotient
  * the reference computes per cell). Call after creating or changing eps/mu. */
@@ -137,17 +154,20 @@ int fdtd_update_j(FdtdPlan *plan, const FdtdBuffers *buf, void *stream, double c
 
 /* Point sources for fdtd_run: after the E update of step t, E[index[k]] += values[t*n + k]
  * (the host-side `sim.E[ind] += field_source(t)` of opencl_fdtd's fdtd.py:168-169, moved on
- * the device). index is a flat index into the 3N E array; values is a device array of
- * nsteps*n elements in the plan's dtype. */
+ * the device; sources on one cell are added in list order). index holds flat indices into
+ * the 3N E array in HOST memory (n <= 64); values is a DEVICE array of nsteps*n elements in
+ * the plan's dtype. */
 typedef struct FdtdPointSources {
     int32_t n;
     int32_t _pad;
-    const int64_t *index;    /* device, n entries */
+    const int64_t *index;    /* host, n entries */
     const void *values;      /* device, nsteps * n entries */
 } FdtdPointSources;
 
 /* Run nsteps canonical steps (fdtd.py:162-175: E, F, point sources, H, G, S) on the stream
- * with no host round trip. src may be NULL. */
+ * with no host round trip. src may be NULL. With the scratch buffers set (and no Bloch
+ * boundaries, at most 8 sources, no overlapping CPML faces) each step is one fused kernel;
+ * oS is then written on the last step only. */
 int fdtd_run(FdtdPlan *plan, const FdtdBuffers *buf, void *stream, int32_t nsteps,
              const FdtdPointSources *src);
 

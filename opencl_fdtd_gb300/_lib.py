@@ -23,6 +23,10 @@ FDTD_ERR_WATCHDOG = -4
 FDTD_ERR_NONFINITE = -5
 FDTD_F32 = 0
 FDTD_F64 = 1
+FDTD_TUNE_XCHUNK = 1
+FDTD_TUNE_SLAB = 2
+FDTD_TUNE_FUSED_CELLS = 3
+FDTD_TUNE_FUSED_XCHUNK = 4
 
 
 class FdtdPmlDesc(ctypes.Structure):
@@ -52,7 +56,8 @@ class FdtdBuffers(ctypes.Structure):
                 ("Jr", c_vp), ("Ji", c_vp),
                 ("psi_e", _PSI), ("psi_h", _PSI), ("psi_f", _PSI), ("psi_g", _PSI),
                 ("inv_de", c_vp * 3), ("inv_dh", c_vp * 3),
-                ("ce", c_vp), ("cm", c_vp)]
+                ("ce", c_vp), ("cm", c_vp),
+                ("E2", c_vp), ("H2", c_vp), ("psi_e2", _PSI), ("psi_h2", _PSI)]
 
 
 class FdtdPointSources(ctypes.Structure):
@@ -66,7 +71,8 @@ SIGNATURES = [
     ("fdtd_last_error", ctypes.c_char_p, []),
     ("fdtd_plan_create", c_i32, [_P(FdtdDesc), _P(c_vp)]),
     ("fdtd_plan_destroy", c_i32, [c_vp]),
-    ("fdtd_plan_tune", c_i32, [c_vp, c_i32]),
+    ("fdtd_plan_tune", c_i32, [c_vp, c_i32, c_i32]),
+    ("fdtd_plan_get", c_i32, [c_vp, c_i32, _P(c_i32)]),
     ("fdtd_prepare", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),
     ("fdtd_update_e", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),
     ("fdtd_update_h", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),

@@ -14,6 +14,7 @@
 #include "yee_common.cuh"
 #include "yee_launch.h"
 #include "fdtd_plan.h"
+#include "fused.h"
 
 using namespace fdtd;
 
@@ -136,7 +137,8 @@ YeeK<R> make_yee(const FdtdPlan *p, bool etype, bool imag, R *P, const R *Q, con
 }
 
 template <typename R>
-int run_update_e(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag)
+int run_update_e(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag,
+                 uint32_t xbeg = 0, uint32_t xend = 0xffffffffu)
 {
     R *P = (R *)(imag ? b->F : b->E);
     const R *Q = (const R *)(imag ? b->G : b->H);
@@ -144,11 +146,14 @@ int run_update_e(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag)
     void *const(*psi)[2] = imag ? b->psi_f : b->psi_e;
     YeeK<R> k = make_yee<R>(p, true, imag, P, Q, Rp, (const R *)b->eps, (const R *)b->ce, nullptr,
                             psi, b->inv_dh);
+    k.xbeg = xbeg;
+    k.xend = xend < p->sx ? xend : p->sx;
     return check_cuda(launch_yee_e<R>(k, st), imag ? "update_F launch" : "update_E launch");
 }
 
 template <typename R>
-int run_update_h(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag)
+int run_update_h(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag,
+                 uint32_t xbeg = 0, uint32_t xend = 0xffffffffu)
 {
     R *P = (R *)(imag ? b->G : b->H);
     const R *Q = (const R *)(imag ? b->F : b->E);
@@ -158,12 +163,15 @@ int run_update_h(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag)
     YeeK<R> k = make_yee<R>(p, false, imag, P, Q, Rp, p->d.has_mu ? (const R *)b->mu : nullptr,
                             p->d.has_mu ? (const R *)b->cm : nullptr,
                             poynt ? (R *)b->oS : nullptr, psi, b->inv_de);
+    k.xbeg = xbeg;
+    k.xend = xend < p->sx ? xend : p->sx;
     return check_cuda(launch_yee_h<R>(k, p->d.has_mu != 0, poynt, st),
                       imag ? "update_G launch" : "update_H launch");
 }
 
 template <typename R>
-int run_update_s(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st)
+int run_update_s(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st,
+                 uint32_t xbeg = 0, uint32_t xend = 0xffffffffu)
 {
     SK<R> k;
     std::memset(&k, 0, sizeof(k));
@@ -176,6 +184,8 @@ int run_update_s(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st)
     k.N = p->N;
     k.dsz = FastDiv::make(p->sz);
     k.xchunk = p->xchunk;
+    k.xbeg = xbeg;
+    k.xend = xend < p->sx ? xend : p->sx;
     const R dt = (R)p->d.dt;
     k.sf = (R)((double)dt * 0.125);  // update_s.cl:33
     return check_cuda(launch_poynting<R>(k, st), "update_S launch");
@@ -225,17 +235,189 @@ int run_update_j(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, double c, d
     return check_cuda(launch_fieldsrc<R>(k, st), "update_J launch");
 }
 
+// Add the sources whose x plane lies in [xbeg, xend) (all when the range is the grid).
 template <typename R>
 int run_point_sources(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st,
-                      const FdtdPointSources *src, int t)
+                      const FdtdPointSources *src, int t, uint32_t xbeg = 0,
+                      uint32_t xend = 0xffffffffu)
 {
     PointK<R> k;
+    std::memset(&k, 0, sizeof(k));
     k.E = (R *)b->E;
-    k.index = src->index;
     k.values = (const R *)src->values;
-    k.n = src->n;
     k.t = t;
+    k.stride = src->n;
+    int n = 0;
+    for (int s = 0; s < src->n; ++s) {
+        const uint32_t plane = (uint32_t)(((uint64_t)src->index[s] % p->N) / p->syz);
+        if (plane < xbeg || plane >= xend) continue;
+        k.index[n] = src->index[s];
+        k.col[n] = s;
+        ++n;
+    }
+    k.n = n;
+    if (!n) return FDTD_OK;
     return check_cuda(launch_point_sources<R>(k, st), "point source launch");
+}
+
+// Per-update kernels over x slabs small enough to stay resident in L2: E on slab s, then H
+// one plane behind (H at x needs E_new at x+1; E at x needs H_old at x-1), then S one plane
+// behind H. Within a step each update's reads of the previous update's output hit L2 while
+// the slab is still there. Every cell is updated by the same kernels as a full-grid launch,
+// so results do not depend on the slab size.
+template <typename R>
+int run_slabs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
+              const FdtdPointSources *src)
+{
+    const uint32_t sx = p->sx;
+    const uint32_t W = p->slab ? p->slab : sx;
+    const bool bloch = p->d.n_bloch != 0, poynt = p->d.do_poynting != 0;
+    int rc;
+    if (W >= sx) {
+        // one slab: the plain whole-grid sequence
+        for (int t = 0; t < nsteps; ++t) {
+            if ((rc = run_update_e<R>(p, b, st, false))) return rc;
+            if (bloch && (rc = run_update_e<R>(p, b, st, true))) return rc;
+            if (src && src->n > 0 && (rc = run_point_sources<R>(p, b, st, src, t))) return rc;
+            if ((rc = run_update_h<R>(p, b, st, false))) return rc;
+            if (bloch && (rc = run_update_h<R>(p, b, st, true))) return rc;
+            if (poynt && (rc = run_update_s<R>(p, b, st))) return rc;
+        }
+        return FDTD_OK;
+    }
+    for (int t = 0; t < nsteps; ++t) {
+        for (uint32_t a = 0; a < sx; a += W) {
+            const uint32_t e = a + W < sx ? a + W : sx;
+            if ((rc = run_update_e<R>(p, b, st, false, a, e))) return rc;
+            if (bloch && (rc = run_update_e<R>(p, b, st, true, a, e))) return rc;
+            if (src && src->n > 0 && (rc = run_point_sources<R>(p, b, st, src, t, a, e))) return rc;
+            const uint32_t h0 = a ? a - 1 : 0, h1 = e - 1;
+            if ((rc = run_update_h<R>(p, b, st, false, h0, h1))) return rc;
+            if (bloch && (rc = run_update_h<R>(p, b, st, true, h0, h1))) return rc;
+            if (poynt && (rc = run_update_s<R>(p, b, st, h0 ? h0 : 1, h1))) return rc;
+        }
+        if ((rc = run_update_h<R>(p, b, st, false, sx - 1, sx))) return rc;
+        if (bloch && (rc = run_update_h<R>(p, b, st, true, sx - 1, sx))) return rc;
+        if (poynt) {
+            if ((rc = run_update_s<R>(p, b, st, sx - 1, sx))) return rc;
+            if (sx > 1 && (rc = run_update_s<R>(p, b, st, 0, 1))) return rc;
+        }
+    }
+    return FDTD_OK;
+}
+
+// Cells of a plane one fused-step block owns: its window (own cells plus one row of sz cells
+// on each side) must fit the block's FUSED_THREADS threads. 0 when a plane row is too long.
+uint32_t fused_cells_of(const FdtdPlan *p)
+{
+    if ((uint64_t)2 * p->sz + 32 > (uint64_t)FUSED_THREADS) return 0;
+    uint32_t J = FUSED_THREADS - 2 * p->sz;
+    if (p->fused_cells && p->fused_cells < J) J = p->fused_cells;
+    return J < p->syz ? J : p->syz;
+}
+
+// Fused multi-step path: one launch per step, reading A and writing B, then swapping.
+template <typename R>
+int run_fused(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
+              const FdtdPointSources *src)
+{
+    FusedK<R> k;
+    std::memset(&k, 0, sizeof(k));
+    k.sx = p->sx;
+    k.sy = p->sy;
+    k.sz = p->sz;
+    k.syz = p->syz;
+    k.N = p->N;
+    k.dsz = FastDiv::make(p->sz);
+    k.dt = (R)p->d.dt;
+    k.inv_d = (R)(1.0 / p->d.dx);
+    k.sf = (R)((double)k.dt * 0.125);
+    for (int r = 0; r < 3; ++r) {
+        k.inv_de[r] = p->d.uniform ? nullptr : (const R *)b->inv_de[r];
+        k.inv_dh[r] = p->d.uniform ? nullptr : (const R *)b->inv_dh[r];
+    }
+    const int dxmode = !p->d.uniform ? 2 : ((R)(1.0 / p->d.dx) == R(1) ? 0 : 1);
+    k.ce = (const R *)b->ce;
+    k.cm = p->d.has_mu ? (const R *)b->cm : nullptr;
+    k.S = (R *)b->S;
+    k.oS = (R *)b->oS;
+    const bool poynt = p->d.do_poynting != 0;
+    if (src && src->n > 0) {
+        k.nsrc = src->n;
+        k.src_values = (const R *)src->values;
+        for (int s = 0; s < src->n; ++s) {
+            const uint64_t ind = (uint64_t)src->index[s];
+            const uint64_t cell = ind % p->N;
+            k.src_c[s] = (int32_t)(ind / p->N);
+            k.src_x[s] = (uint32_t)(cell / p->syz);
+            k.src_y[s] = (uint32_t)((cell % p->syz) / p->sz);
+            k.src_z[s] = (uint32_t)(cell % p->sz);
+        }
+    }
+    k.J = fused_cells_of(p);
+    k.xchunk = p->fused_xchunk;
+    k.ldE = k.J + 2 * p->sz;
+    k.ldH = k.J + p->sz;
+    // face index per axis/side, for the psi pointers of each step
+    int fidx[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
+    for (int f = 0; f < p->d.n_pml; ++f) {
+        const FdtdPmlDesc &pd = p->d.pml[f];
+        const uint32_t sa = pd.axis == 0 ? p->sx : pd.axis == 1 ? p->sy : p->sz;
+        FAxis<R> &a = k.ax[pd.axis];
+        if (pd.polarity == 1 && (uint32_t)pd.thickness > sa) continue;  // never applies
+        const int side = pd.polarity;
+        if (side == 0) a.Tn = pd.thickness;
+        else a.Tp = pd.thickness;
+        for (int c = 0; c < 3; ++c) {
+            a.tab[0][side][c] = (const R *)p->tab[f][c];
+            a.tab[1][side][c] = (const R *)p->tab[f][3 + c];
+        }
+        fidx[pd.axis][side] = f;
+    }
+    void *E[2] = {b->E, b->E2}, *H[2] = {b->H, b->H2};
+    for (int t = 0; t < nsteps; ++t) {
+        const int a = t & 1, o = a ^ 1;
+        k.EA = (const R *)E[a];
+        k.HA = (const R *)H[a];
+        k.EB = (R *)E[o];
+        k.HB = (R *)H[o];
+        for (int r = 0; r < 3; ++r)
+            for (int side = 0; side < 2; ++side) {
+                const int f = fidx[r][side];
+                if (f < 0) continue;
+                void *const *pe_a = a ? b->psi_e2[f] : b->psi_e[f];
+                void *const *ph_a = a ? b->psi_h2[f] : b->psi_h[f];
+                void *const *pe_o = o ? b->psi_e2[f] : b->psi_e[f];
+                void *const *ph_o = o ? b->psi_h2[f] : b->psi_h[f];
+                for (int c = 0; c < 2; ++c) {
+                    k.ax[r].psiA[0][side][c] = (const R *)pe_a[c];
+                    k.ax[r].psiA[1][side][c] = (const R *)ph_a[c];
+                    k.ax[r].psiB[0][side][c] = (R *)pe_o[c];
+                    k.ax[r].psiB[1][side][c] = (R *)ph_o[c];
+                }
+            }
+        k.t = t;
+        k.write_oS = poynt && t == nsteps - 1;
+        int rc = check_cuda(launch_fused<R>(k, p->d.has_mu != 0, poynt, dxmode, st), "fused step launch");
+        if (rc) return rc;
+    }
+    if (nsteps & 1) {
+        // the last step wrote the scratch copies: bring the state home
+        const size_t fb = 3 * (size_t)p->N * p->elem;
+        int rc = check_cuda(cudaMemcpyAsync(b->E, b->E2, fb, cudaMemcpyDeviceToDevice, st), "copy E");
+        if (!rc) rc = check_cuda(cudaMemcpyAsync(b->H, b->H2, fb, cudaMemcpyDeviceToDevice, st), "copy H");
+        for (int f = 0; !rc && f < p->d.n_pml; ++f) {
+            const FdtdPmlDesc &pd = p->d.pml[f];
+            size_t cells = (size_t)p->N / (pd.axis == 0 ? p->sx : pd.axis == 1 ? p->sy : p->sz);
+            const size_t pb = cells * (size_t)pd.thickness * p->elem;
+            for (int c = 0; !rc && c < 2 && pb; ++c) {
+                rc = check_cuda(cudaMemcpyAsync(b->psi_e[f][c], b->psi_e2[f][c], pb, cudaMemcpyDeviceToDevice, st), "copy psi_e");
+                if (!rc) rc = check_cuda(cudaMemcpyAsync(b->psi_h[f][c], b->psi_h2[f][c], pb, cudaMemcpyDeviceToDevice, st), "copy psi_h");
+            }
+        }
+        if (rc) return rc;
+    }
+    return FDTD_OK;
 }
 
 }  // namespace fdtd
@@ -298,6 +480,27 @@ int check_psi(const FdtdPlan *p, void *const psi[6][2], const char *what)
     return FDTD_OK;
 }
 
+// The fused step covers the common case: no Bloch boundaries, CPML faces of one axis
+// disjoint, dt/eps (and dt/mu) caches and every scratch buffer present, few point sources,
+// and a per-block window that fits in shared memory.
+bool fused_eligible(const FdtdPlan *p, const FdtdBuffers *b, const FdtdPointSources *src)
+{
+    if (p->d.n_bloch || !faces_disjoint(p)) return false;
+    if (!b->ce || (p->d.has_mu && !b->cm)) return false;
+    if (!b->E2 || !b->H2) return false;
+    if (p->d.do_poynting && (!b->S || !b->oS)) return false;
+    if (!p->d.uniform && (!b->inv_de[0] || !b->inv_dh[0])) return false;
+    for (int f = 0; f < p->d.n_pml; ++f)
+        if (p->d.pml[f].thickness > 0 &&
+            (!b->psi_e2[f][0] || !b->psi_e2[f][1] || !b->psi_h2[f][0] || !b->psi_h2[f][1]))
+            return false;
+    if (src && src->n > FUSED_MAX_SRC) return false;
+    const uint32_t J = fused_cells_of(p);
+    if (J == 0) return false;
+    const size_t smem = (6 * (size_t)(J + 2 * p->sz) + 6 * (size_t)(J + p->sz)) * p->elem;
+    return smem <= 200 * 1024;
+}
+
 int check_inv(const FdtdPlan *p, const void *const inv[3], const char *what)
 {
     if (p->d.uniform) return FDTD_OK;
@@ -331,7 +534,12 @@ int fdtd_plan_create(const FdtdDesc *desc, FdtdPlan **out)
     p->syz = p->sy * p->sz;
     p->N = (uint64_t)p->sx * p->syz;
     p->elem = desc->dtype == FDTD_F64 ? 8 : 4;
-    p->xchunk = 16;
+    p->xchunk = 8;
+    // Whole-grid launches measured fastest on GB300 for the 395x345x73 workload (0.33 ms per
+    // step against 0.43-0.86 ms for 48- to 8-plane slabs), so slabs are opt-in.
+    p->slab = 0;
+    p->fused_cells = 0;
+    p->fused_xchunk = 16;
     cudaGetDevice(&p->device);
     size_t total = 0;
     for (int f = 0; f < desc->n_pml; ++f) total += 6 * (size_t)desc->pml[f].thickness;
@@ -374,12 +582,42 @@ int fdtd_plan_destroy(FdtdPlan *plan)
     return FDTD_OK;
 }
 
-int fdtd_plan_tune(FdtdPlan *p, int32_t xchunk)
+int fdtd_plan_tune(FdtdPlan *p, int32_t key, int32_t value)
 {
     if (!p) return fail(FDTD_ERR_INVALID, "plan is NULL");
-    if (xchunk < 1 || xchunk > 4096) return fail(FDTD_ERR_INVALID, "xchunk must be in [1, 4096]");
-    p->xchunk = xchunk;
-    return FDTD_OK;
+    switch (key) {
+    case FDTD_TUNE_XCHUNK:
+        if (value < 1 || value > 4096) return fail(FDTD_ERR_INVALID, "xchunk must be in [1, 4096]");
+        p->xchunk = value;
+        return FDTD_OK;
+    case FDTD_TUNE_SLAB:
+        if (value < 0) return fail(FDTD_ERR_INVALID, "slab must be >= 0 (0: whole grid)");
+        p->slab = (uint32_t)value;
+        return FDTD_OK;
+    case FDTD_TUNE_FUSED_CELLS:
+        if (value < 0 || value > 8192 || (value % 32))
+            return fail(FDTD_ERR_INVALID, "fused_cells must be 0 or a multiple of 32 up to 8192");
+        p->fused_cells = (uint32_t)value;
+        return FDTD_OK;
+    case FDTD_TUNE_FUSED_XCHUNK:
+        if (value < 1 || value > 4096) return fail(FDTD_ERR_INVALID, "fused_xchunk must be in [1, 4096]");
+        p->fused_xchunk = (uint32_t)value;
+        return FDTD_OK;
+    default:
+        return fail(FDTD_ERR_INVALID, "unknown tuning key");
+    }
+}
+
+int fdtd_plan_get(const FdtdPlan *p, int32_t key, int32_t *value)
+{
+    if (!p || !value) return fail(FDTD_ERR_INVALID, "plan or value is NULL");
+    switch (key) {
+    case FDTD_TUNE_XCHUNK: *value = p->xchunk; return FDTD_OK;
+    case FDTD_TUNE_SLAB: *value = (int32_t)p->slab; return FDTD_OK;
+    case FDTD_TUNE_FUSED_CELLS: *value = (int32_t)p->fused_cells; return FDTD_OK;
+    case FDTD_TUNE_FUSED_XCHUNK: *value = (int32_t)p->fused_xchunk; return FDTD_OK;
+    default: return fail(FDTD_ERR_INVALID, "unknown tuning key");
+    }
 }
 
 int fdtd_prepare(FdtdPlan *p, const FdtdBuffers *b, void *stream)
@@ -390,6 +628,20 @@ int fdtd_prepare(FdtdPlan *p, const FdtdBuffers *b, void *stream)
     if (p->d.has_mu && b->cm && !b->mu) return fail(FDTD_ERR_INVALID, "prepare: mu is required to fill cm");
     cudaStream_t st = (cudaStream_t)stream;
     return p->d.dtype == FDTD_F64 ? run_prepare<double>(p, b, st) : run_prepare<float>(p, b, st);
+}
+
+// The buffer checks of every update fdtd_run performs.
+static int check_run_buffers(FdtdPlan *p, const FdtdBuffers *b)
+{
+    int rc;
+    if (!b->E || !b->H || !b->eps) return fail(FDTD_ERR_INVALID, "fdtd_run: E, H and eps are required");
+    if (p->d.n_bloch && (!b->F || !b->G)) return fail(FDTD_ERR_INVALID, "fdtd_run: F and G are required with Bloch boundaries");
+    if (p->d.has_mu && !b->mu) return fail(FDTD_ERR_INVALID, "fdtd_run: mu is required");
+    if (p->d.do_poynting && (!b->S || !b->oS)) return fail(FDTD_ERR_INVALID, "fdtd_run: S and oS are required with Poynting");
+    if ((rc = check_psi(p, b->psi_e, "fdtd_run")) || (rc = check_psi(p, b->psi_h, "fdtd_run"))) return rc;
+    if (p->d.n_bloch && ((rc = check_psi(p, b->psi_f, "fdtd_run")) || (rc = check_psi(p, b->psi_g, "fdtd_run")))) return rc;
+    if ((rc = check_inv(p, b->inv_dh, "fdtd_run")) || (rc = check_inv(p, b->inv_de, "fdtd_run"))) return rc;
+    return FDTD_OK;
 }
 
 int fdtd_update_e(FdtdPlan *p, const FdtdBuffers *b, void *stream)
@@ -489,20 +741,22 @@ int fdtd_run(FdtdPlan *p, const FdtdBuffers *b, void *stream, int32_t nsteps,
     if (nsteps < 0) return fail(FDTD_ERR_INVALID, "fdtd_run: nsteps must be >= 0");
     if (src && src->n > 0 && (!src->index || !src->values))
         return fail(FDTD_ERR_INVALID, "fdtd_run: source index/values pointer is NULL");
+    if (src && src->n > MAX_POINT_SOURCES)
+        return fail(FDTD_ERR_INVALID, "fdtd_run: at most 64 point sources");
+    for (int s = 0; src && s < src->n; ++s)
+        if (src->index[s] < 0 || (uint64_t)src->index[s] >= 3 * p->N)
+            return fail(FDTD_ERR_INVALID, "fdtd_run: point source index out of range");
     const bool f64 = p->d.dtype == FDTD_F64;
-    for (int t = 0; t < nsteps; ++t) {
-        if ((rc = fdtd_update_e(p, b, stream))) return rc;
-        if (p->d.n_bloch && (rc = fdtd_update_f(p, b, stream))) return rc;
-        if (src && src->n > 0) {
-            rc = f64 ? run_point_sources<double>(p, b, (cudaStream_t)stream, src, t)
-                     : run_point_sources<float>(p, b, (cudaStream_t)stream, src, t);
-            if (rc) return rc;
-        }
-        if ((rc = fdtd_update_h(p, b, stream))) return rc;
-        if (p->d.n_bloch && (rc = fdtd_update_g(p, b, stream))) return rc;
-        if (p->d.do_poynting && (rc = fdtd_update_s(p, b, stream))) return rc;
+    if (fused_eligible(p, b, src)) {
+        if ((rc = check_psi(p, b->psi_e, "fdtd_run")) || (rc = check_psi(p, b->psi_h, "fdtd_run")))
+            return rc;
+        cudaStream_t st = (cudaStream_t)stream;
+        return f64 ? run_fused<double>(p, b, st, nsteps, src) : run_fused<float>(p, b, st, nsteps, src);
     }
-    return FDTD_OK;
+    // validate once with the per-update entry points' checks, then run the slab schedule
+    if ((rc = check_run_buffers(p, b))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    return f64 ? run_slabs<double>(p, b, st, nsteps, src) : run_slabs<float>(p, b, st, nsteps, src);
 }
 
 }  // extern "C"

@@ -13,6 +13,9 @@ struct FdtdPlan {
     size_t elem;                // bytes per element of the plan's dtype
     int device;                 // device that was current at creation
     int32_t xchunk;             // x planes a bulk-kernel thread marches
+    uint32_t slab;              // x planes per L2-resident slab in fdtd_run (0: whole grid)
+    uint32_t fused_cells;       // plane cells one block of the fused step owns
+    uint32_t fused_xchunk;      // x planes one block of the fused step marches
     void *coef = nullptr;       // device copy of every face's six coefficient tables
     const void *tab[6][6];      // per face: p0e p1e p2e p0h p1h p2h (device pointers)
 };

@@ -80,6 +80,7 @@ struct YeeK {
     AxisK<R> ax[3];
     FastDiv dsz;
     int32_t xchunk, bulk;
+    uint32_t xbeg, xend;        // planes [xbeg, xend) this launch updates
 };
 
 template <typename R>
@@ -91,6 +92,7 @@ struct SK {
     R sf;
     FastDiv dsz;
     int32_t xchunk, _pad;
+    uint32_t xbeg, xend;        // planes [xbeg, xend) this launch updates
 };
 
 template <typename R>
@@ -104,12 +106,15 @@ struct JK {
     R c, s;
 };
 
+constexpr int MAX_POINT_SOURCES = 64;
+
 template <typename R>
 struct PointK {
     R *E;
-    const int64_t *index;
-    const R *values;
-    int32_t n, t;
+    const R *values;            // [nsteps][stride]
+    int32_t n, t, stride, _pad;
+    int64_t index[MAX_POINT_SOURCES];
+    int32_t col[MAX_POINT_SOURCES];   // column of each source in values
 };
 
 template <typename R>

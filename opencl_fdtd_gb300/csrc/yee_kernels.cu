@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(BLOCK) k_generic_e(const YeeK<R> k)
     const uint32_t j = blockIdx.x * BLOCK + threadIdx.x;
     if (j >= k.syz) return;
     const uint32_t y = k.dsz.div(j);
-    cell_e<R>(k, blockIdx.y, y, j - y * k.sz);
+    cell_e<R>(k, k.xbeg + blockIdx.y, y, j - y * k.sz);
 }
 
 template <typename R, bool MU, bool POYNT>
@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(BLOCK) k_generic_h(const YeeK<R> k)
     const uint32_t j = blockIdx.x * BLOCK + threadIdx.x;
     if (j >= k.syz) return;
     const uint32_t y = k.dsz.div(j);
-    cell_h<R, MU, POYNT>(k, blockIdx.y, y, j - y * k.sz);
+    cell_h<R, MU, POYNT>(k, k.xbeg + blockIdx.y, y, j - y * k.sz);
 }
 
 // ---- bulk kernels ----------------------------------------------------------------------------
@@ -352,8 +352,8 @@ __global__ void __launch_bounds__(BLOCK, 3) k_bulk_e(const YeeK<R> k)
     const uint32_t sx = k.sx, sy = k.sy, sz = k.sz, syz = k.syz;
     const uint32_t y = k.dsz.div(j);
     const uint32_t z = j - y * sz;
-    const uint32_t xa = blockIdx.y * (uint32_t)k.xchunk;
-    const uint32_t xb = min(xa + (uint32_t)k.xchunk, sx);
+    const uint32_t xa = k.xbeg + blockIdx.y * (uint32_t)k.xchunk;
+    const uint32_t xb = min(xa + (uint32_t)k.xchunk, k.xend);
     const uint64_t N = k.N;
     const R *__restrict__ Qx = k.Q;
     const R *__restrict__ Qy = k.Q + N;
@@ -484,8 +484,8 @@ __global__ void __launch_bounds__(BLOCK, 3) k_bulk_h(const YeeK<R> k)
     const uint32_t sx = k.sx, sy = k.sy, sz = k.sz, syz = k.syz;
     const uint32_t y = k.dsz.div(j);
     const uint32_t z = j - y * sz;
-    const uint32_t xa = blockIdx.y * (uint32_t)k.xchunk;
-    const uint32_t xb = min(xa + (uint32_t)k.xchunk, sx);
+    const uint32_t xa = k.xbeg + blockIdx.y * (uint32_t)k.xchunk;
+    const uint32_t xb = min(xa + (uint32_t)k.xchunk, k.xend);
     const uint64_t N = k.N;
     const R *__restrict__ Qx = k.Q;
     const R *__restrict__ Qy = k.Q + N;
@@ -631,8 +631,8 @@ __global__ void __launch_bounds__(BLOCK) k_bulk_s(const SK<R> k)
     const uint32_t sx = k.sx, sy = k.sy, sz = k.sz, syz = k.syz;
     const uint32_t y = k.dsz.div(j);
     const uint32_t z = j - y * sz;
-    const uint32_t xa = blockIdx.y * (uint32_t)k.xchunk;
-    const uint32_t xb = min(xa + (uint32_t)k.xchunk, sx);
+    const uint32_t xa = k.xbeg + blockIdx.y * (uint32_t)k.xchunk;
+    const uint32_t xb = min(xa + (uint32_t)k.xchunk, k.xend);
     const uint64_t N = k.N;
     const R *__restrict__ oxy = k.oS;
     const R *__restrict__ oyz = k.oS + N;
@@ -700,34 +700,38 @@ __global__ void __launch_bounds__(BLOCK) k_fieldsrc(const JK<R> k)
 }
 
 // ---- point sources of fdtd_run: E[index] += value (fdtd.py:168-169) ------------------------
+// One thread adds every source in list order, so sources sharing a cell accumulate in the
+// same order as successive host-side additions.
 template <typename R>
 __global__ void k_point_sources(const PointK<R> k)
 {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= k.n) return;
-    const int64_t ind = k.index[s];
-    k.E[ind] = k.E[ind] + k.values[(int64_t)k.t * k.n + s];
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int s = 0; s < k.n; ++s) {
+        const int64_t ind = k.index[s];
+        k.E[ind] = k.E[ind] + k.values[(int64_t)k.t * k.stride + k.col[s]];
+    }
 }
 
 // ---- launchers ------------------------------------------------------------------------------
-static inline dim3 bulk_grid(uint32_t syz, uint32_t sx, int xchunk)
+static inline dim3 bulk_grid(uint32_t syz, uint32_t nx, int xchunk)
 {
-    return dim3((syz + BLOCK - 1) / BLOCK, (sx + (uint32_t)xchunk - 1) / (uint32_t)xchunk, 1);
+    return dim3((syz + BLOCK - 1) / BLOCK, (nx + (uint32_t)xchunk - 1) / (uint32_t)xchunk, 1);
 }
 
-static inline dim3 plane_grid(uint32_t syz, uint32_t sx)
+static inline dim3 plane_grid(uint32_t syz, uint32_t nx)
 {
-    return dim3((syz + BLOCK - 1) / BLOCK, sx, 1);
+    return dim3((syz + BLOCK - 1) / BLOCK, nx, 1);
 }
 
 template <typename R>
 cudaError_t launch_yee_e(const YeeK<R> &k, cudaStream_t st)
 {
+    if (k.xend <= k.xbeg) return cudaSuccess;
     if (!k.bulk) {
-        k_generic_e<R><<<plane_grid(k.syz, k.sx), BLOCK, 0, st>>>(k);
+        k_generic_e<R><<<plane_grid(k.syz, k.xend - k.xbeg), BLOCK, 0, st>>>(k);
         return cudaGetLastError();
     }
-    const dim3 g = bulk_grid(k.syz, k.sx, k.xchunk);
+    const dim3 g = bulk_grid(k.syz, k.xend - k.xbeg, k.xchunk);
     if (k.bloch_mask) {
         if (k.dxmode == 0) k_bulk_e<R, 0, true><<<g, BLOCK, 0, st>>>(k);
         else if (k.dxmode == 1) k_bulk_e<R, 1, true><<<g, BLOCK, 0, st>>>(k);
@@ -743,7 +747,7 @@ cudaError_t launch_yee_e(const YeeK<R> &k, cudaStream_t st)
 template <typename R, int DX, bool BLOCH>
 static void bulk_h(const YeeK<R> &k, bool mu, bool poynting, cudaStream_t st)
 {
-    const dim3 g = bulk_grid(k.syz, k.sx, k.xchunk);
+    const dim3 g = bulk_grid(k.syz, k.xend - k.xbeg, k.xchunk);
     if (mu) {
         if (poynting) k_bulk_h<R, DX, true, true, BLOCH><<<g, BLOCK, 0, st>>>(k);
         else k_bulk_h<R, DX, true, false, BLOCH><<<g, BLOCK, 0, st>>>(k);
@@ -763,8 +767,9 @@ static void bulk_h_dispatch(const YeeK<R> &k, bool mu, bool poynting, cudaStream
 template <typename R>
 cudaError_t launch_yee_h(const YeeK<R> &k, bool mu, bool poynting, cudaStream_t st)
 {
+    if (k.xend <= k.xbeg) return cudaSuccess;
     if (!k.bulk) {
-        const dim3 g = plane_grid(k.syz, k.sx);
+        const dim3 g = plane_grid(k.syz, k.xend - k.xbeg);
         if (mu) {
             if (poynting) k_generic_h<R, true, true><<<g, BLOCK, 0, st>>>(k);
             else k_generic_h<R, true, false><<<g, BLOCK, 0, st>>>(k);
@@ -783,7 +788,8 @@ cudaError_t launch_yee_h(const YeeK<R> &k, bool mu, bool poynting, cudaStream_t 
 template <typename R>
 cudaError_t launch_poynting(const SK<R> &k, cudaStream_t st)
 {
-    k_bulk_s<R><<<bulk_grid(k.syz, k.sx, k.xchunk), BLOCK, 0, st>>>(k);
+    if (k.xend <= k.xbeg) return cudaSuccess;
+    k_bulk_s<R><<<bulk_grid(k.syz, k.xend - k.xbeg, k.xchunk), BLOCK, 0, st>>>(k);
     return cudaGetLastError();
 }
 
@@ -810,7 +816,7 @@ template <typename R>
 cudaError_t launch_point_sources(const PointK<R> &k, cudaStream_t st)
 {
     if (k.n <= 0) return cudaSuccess;
-    k_point_sources<R><<<(k.n + 127) / 128, 128, 0, st>>>(k);
+    k_point_sources<R><<<1, 32, 0, st>>>(k);
     return cudaGetLastError();
 }
 

@@ -201,6 +201,7 @@ class Simulation:
         self._mat_key = None
         self._buf_key = None
         self._buf = _lib.FdtdBuffers()
+        self._scratch = None
         self.steps_run = 0
 
         self.update_E = self._create_operation(self._lib.fdtd_update_e)
@@ -388,9 +389,36 @@ class Simulation:
         if self._cm is not None:
             b.cm = self._cm.data_ptr()
         self._buf = b
+        self._attach_scratch()
         self._buf_key = key
         self._prepare((self.eps._version, None if self.mu is None else self.mu._version))
         return b
+
+    def _attach_scratch(self, on: bool = True):
+        b = self._buf
+        if on and self._scratch is not None:
+            E2, H2, pe2, ph2 = self._scratch
+            b.E2, b.H2 = E2.data_ptr(), H2.data_ptr()
+            for f, (u, v) in enumerate(pe2):
+                b.psi_e2[f][0], b.psi_e2[f][1] = u.data_ptr(), v.data_ptr()
+            for f, (u, v) in enumerate(ph2):
+                b.psi_h2[f][0], b.psi_h2[f][1] = u.data_ptr(), v.data_ptr()
+        else:
+            b.E2 = b.H2 = None
+            for f in range(6):
+                for c in range(2):
+                    b.psi_e2[f][c] = None
+                    b.psi_h2[f][c] = None
+
+    def _ensure_scratch(self):
+        """Second copies of E, H and the CPML arrays, read and written alternately by the fused
+        multi-step kernel (allocated on the first fused run, kept for later ones)."""
+        if self._scratch is None:
+            E2 = torch.empty_like(self.E)
+            H2 = torch.empty_like(self.H)
+            pe2 = [(torch.empty_like(u), torch.empty_like(v)) for u, v in self.psi["E"]]
+            ph2 = [(torch.empty_like(u), torch.empty_like(v)) for u, v in self.psi["H"]]
+            self._scratch = (E2, H2, pe2, ph2)
 
     def _prepare(self, mat_key):
         _lib.check(self._lib.fdtd_prepare(self._plan, ctypes.byref(self._buf),
@@ -428,18 +456,26 @@ class Simulation:
     # ------------------------------------------------------------------------------------
     # additions beyond the reference
     # ------------------------------------------------------------------------------------
-    def run(self, nsteps: int, point_sources=None, wait_for=None) -> Event:
+    def run(self, nsteps: int, point_sources=None, wait_for=None, fused: bool = False) -> Event:
         """Advance ``nsteps`` canonical steps (E, F, point sources, H, G, S) in one call.
 
         ``point_sources`` is a list of (flat_index, values) pairs: after the E update of step
         t, ``E[flat_index] += values[t]`` (fdtd.py:168-169 without the host round trip).
-        values are rounded to the field dtype, as the host-side ``+=`` does."""
+        values are rounded to the field dtype, as the host-side ``+=`` does.
+
+        By default each step runs the per-update kernels (optionally over L2-resident x slabs,
+        see tune(slab=...)). With ``fused`` and no Bloch boundaries each step is instead one
+        fused kernel (E, sources, H and S in one pass, reading one copy of E, H and the CPML
+        arrays and writing a second); it moves about half the bytes but measured slower on
+        GB300. All give identical fields; the fused path refreshes oS on the last step only."""
         nsteps = int(nsteps)
         stream = self._stream_handle(wait_for)
         src = None
         keep = []
         if point_sources:
             n = len(point_sources)
+            if n > 64:
+                raise ValueError("at most 64 point sources")
             idx = numpy.array([int(i) for i, _ in point_sources], dtype=numpy.int64)
             if (idx < 0).any() or (idx >= 3 * self.N).any():
                 raise IndexError("point source index out of range")
@@ -450,17 +486,37 @@ class Simulation:
                     raise ValueError("point source {} has {} values for {} steps".format(k, v.size, nsteps))
                 vals[:, k] = v[:nsteps]
             with torch.cuda.stream(stream):
-                idx_t = torch.from_numpy(idx).to(self.device, non_blocking=False)
                 val_t = torch.from_numpy(vals).to(self.device, non_blocking=False)
-            keep = [idx_t, val_t]
-            src = _lib.FdtdPointSources(n, 0, idx_t.data_ptr(), val_t.data_ptr())
-        _lib.check(self._lib.fdtd_run(self._plan, ctypes.byref(self._buffers()),
+            idx_host = (ctypes.c_int64 * n)(*idx.tolist())
+            keep = [val_t]
+            src = _lib.FdtdPointSources(n, 0, ctypes.addressof(idx_host), val_t.data_ptr())
+        use_fused = fused and not self.bloch_boundaries
+        if use_fused:
+            self._ensure_scratch()
+        bufs = self._buffers()
+        self._attach_scratch(use_fused)
+        _lib.check(self._lib.fdtd_run(self._plan, ctypes.byref(bufs),
                                       ctypes.c_void_p(stream.cuda_stream), nsteps,
                                       ctypes.byref(src) if src is not None else None))
         for t in keep:
             t.record_stream(stream)
         self.steps_run += nsteps
         return Event(stream)
+
+    def slab_planes(self) -> int:
+        """x planes per slab of run()'s per-update schedule (whole grid when 0)."""
+        v = ctypes.c_int32()
+        _lib.check(self._lib.fdtd_plan_get(self._plan, _lib.FDTD_TUNE_SLAB, ctypes.byref(v)))
+        return v.value or self.shape[0]
+
+    def tune(self, xchunk: int = None, slab: int = None, fused_cells: int = None,
+             fused_xchunk: int = None):
+        """Kernel tiling (None keeps a value); results do not depend on it."""
+        for key, val in ((_lib.FDTD_TUNE_XCHUNK, xchunk), (_lib.FDTD_TUNE_SLAB, slab),
+                         (_lib.FDTD_TUNE_FUSED_CELLS, fused_cells),
+                         (_lib.FDTD_TUNE_FUSED_XCHUNK, fused_xchunk)):
+            if val is not None:
+                _lib.check(self._lib.fdtd_plan_tune(self._plan, key, int(val)))
 
     def get(self, name: str) -> numpy.ndarray:
         """Host copy of a field (what ``pyopencl.array.Array.get()`` returns)."""

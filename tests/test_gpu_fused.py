@@ -1,0 +1,141 @@
+"""The fused multi-step kernel (Simulation.run with fused=True) against the per-call drop-in
+loop and the oracle: bit-identical E, H, S and CPML state for every tiling, including tiles
+so small that the halo and wrap-around recomputation paths run."""
+import copy
+import math
+import os
+
+import numpy
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import port  # noqa: E402
+from opencl_fdtd_gb300 import geometry  # noqa: E402
+from tests.golden import cases  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu(**kw):
+    from opencl_fdtd_gb300 import Simulation
+    return Simulation(**kw)
+
+
+def _np(a):
+    return a.detach().cpu().numpy().reshape(-1)
+
+
+def _sources(kw, loop, nsteps):
+    shape = kw["epsilon"][0].shape
+    N = int(numpy.prod(shape))
+    return [(int(numpy.ravel_multi_index(p, shape)) + c * N,
+             [cases._WAVES[w](t) for t in range(nsteps)]) for p, c, w in loop["sources"]]
+
+
+def _same_state(a, b, poynting):
+    for k in ("E", "H") + (("S", "oS") if poynting else ()):
+        x, y = _np(getattr(a, k)), _np(getattr(b, k))
+        bad = numpy.flatnonzero(x != y)
+        assert bad.size == 0, (k, bad[:5], x[bad[:5]], y[bad[:5]])
+    for fld in "EH":
+        for (u1, v1), (u2, v2) in zip(a.psi[fld], b.psi[fld]):
+            assert torch.equal(u1, u2) and torch.equal(v1, v2), fld
+
+
+@pytest.mark.parametrize("name", ["c1_small", "pml_mixed", "periodic_pec_poynting", "nonuniform",
+                                  "dx_half", "f64_mixed"])
+@pytest.mark.parametrize("tiles", [(0, 0), (32, 3), (64, 1), (96, 2)])
+@pytest.mark.parametrize("nsteps", [7, 10])
+def test_fused_equals_per_call_loop(name, tiles, nsteps):
+    kw, loop = cases.build(name)
+    src = _sources(kw, loop, nsteps)
+    a = _gpu(**copy.deepcopy(kw))
+    b = _gpu(**copy.deepcopy(kw))
+    if tiles[0]:
+        b.tune(fused_cells=tiles[0], fused_xchunk=tiles[1])
+    a.run(nsteps, point_sources=src, fused=False)
+    b.run(nsteps, point_sources=src, fused=True)
+    _same_state(a, b, kw.get("do_poynting", True))
+
+
+def test_fused_matches_oracle_with_mu_and_sources():
+    shape = (18, 16, 20)
+    eps, mu = geometry.sphere_inclusions(shape, n=4, rmin=2, rmax=5, seed=21, pec_index=0)
+    pmls = [{"axis": a, "polarity": p, "thickness": 3} for a in "xyz" for p in "np"]
+    N = int(numpy.prod(shape))
+    steps = 25
+    srcs = [(int(numpy.ravel_multi_index((9, 8, 10), shape)) + 2 * N, [math.sin(0.4 * t) for t in range(steps)]),
+            (int(numpy.ravel_multi_index((4, 12, 5), shape)) + 0 * N, [math.cos(0.3 * t) for t in range(steps)]),
+            (int(numpy.ravel_multi_index((9, 8, 10), shape)) + 2 * N, [0.5] * steps)]
+    kw = dict(epsilon=eps, mu=mu, pmls=pmls, do_poynting=True)
+    g = _gpu(**copy.deepcopy(kw))
+    g.tune(fused_cells=64, fused_xchunk=4)
+    g.run(steps, point_sources=srcs, fused=True)
+    c = port.PortSimulation(nthreads=os.cpu_count(), **copy.deepcopy(kw))
+    for t in range(steps):
+        c.update_E()
+        for ind, vals in srcs:
+            c.E[ind] = c.E[ind] + numpy.float32(vals[t])
+        c.update_H()
+        c.update_S()
+    for k in ("E", "H", "S", "oS"):
+        assert numpy.array_equal(_np(getattr(g, k)), getattr(c, k).reshape(-1)), k
+
+
+def test_fused_then_per_call_continue_identically():
+    """State left by a fused run (odd step count: copied back from the scratch buffers) is
+    the full state: per-call steps after it match an all-per-call history."""
+    kw, loop = cases.build("pml_mixed")
+    src = _sources(kw, loop, 9)
+    a = _gpu(**copy.deepcopy(kw))
+    b = _gpu(**copy.deepcopy(kw))
+    a.run(9, point_sources=src, fused=False)
+    b.run(9, point_sources=src, fused=True)
+    for s in (a, b):
+        for _ in range(4):
+            s.update_E([])
+            s.update_H([])
+            s.update_S([])
+    _same_state(a, b, True)
+
+
+SLAB_CASES = [n for n in cases.CASE_NAMES if n != "fieldsrc"]
+
+
+@pytest.mark.parametrize("name", SLAB_CASES)
+@pytest.mark.parametrize("slab", [1, 2, 5, 0])
+def test_slab_schedule_equals_per_call_loop(name, slab):
+    """run(fused=False) advances the update kernels over x slabs (E, then H one plane
+    behind, then S); every slab width gives the per-call loop's state bit for bit."""
+    kw, loop = cases.build(name)
+    n = loop["steps"]
+    a = cases.run_case(_gpu, name)
+    b = _gpu(**copy.deepcopy(kw))
+    b.tune(slab=slab)
+    b.run(n, point_sources=_sources(kw, loop, n), fused=False)
+    for k, v in cases.outputs(a, name).items():
+        assert numpy.array_equal(v, _np(getattr(b, k))), k
+    for fld in ("EHFG" if kw.get("bloch_boundaries") else "EH"):
+        for (u1, v1), (u2, v2) in zip(a.psi[fld], b.psi[fld]):
+            assert torch.equal(u1, u2) and torch.equal(v1, v2), fld
+
+
+def test_slab_schedule_bloch_mu():
+    shape = (14, 12, 20)
+    rng = numpy.random.default_rng(8)
+    eps, mu = geometry.sphere_inclusions(shape, n=3, rmin=2, rmax=4, seed=4)
+    init = {k: [rng.standard_normal(shape).astype(numpy.float32) for _ in range(3)] for k in "EHFG"}
+    bloch = [{"axis": "x", "real": math.cos(0.3), "imag": math.sin(0.3)},
+             {"axis": "z", "real": math.cos(0.7), "imag": math.sin(0.7)}]
+    pmls = [{"axis": "y", "polarity": p, "thickness": 3} for p in "np"]
+    kw = dict(epsilon=eps, mu=mu, pmls=pmls, bloch_boundaries=bloch, initial_fields=init, do_poynting=True)
+    a = _gpu(**copy.deepcopy(kw))
+    for _ in range(12):
+        a.update_E([]); a.update_F([]); a.update_H([]); a.update_G([]); a.update_S([])
+    for slab in (1, 3, 0):
+        b = _gpu(**copy.deepcopy(kw))
+        b.tune(slab=slab)
+        b.run(12)
+        for k in ("E", "H", "F", "G", "S"):
+            assert torch.equal(getattr(a, k), getattr(b, k)), (slab, k)
