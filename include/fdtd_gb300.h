@@ -164,12 +164,45 @@ typedef struct FdtdPointSources {
     const void *values;      /* device, nsteps * n entries */
 } FdtdPointSources;
 
+/* FP64 DFT point monitor. After each step (E fully updated, point sources included) the
+ * sample x = E[index[p]] is taken at time (step + 1) * dt and accum[p][f] += x *
+ * exp(-i omega[f] (step + 1) dt) in double; with series set, x is also stored in row
+ * series_row of series ([rows][n_points] doubles). All pointers are device pointers. */
+typedef struct FdtdDftMonitor {
+    int32_t n_points, n_freq;
+    const int64_t *index;    /* n_points flat indices into the 3N E array */
+    const double *omega;     /* n_freq angular frequencies, radians per unit time */
+    double *accum;           /* n_points * n_freq * 2 doubles (re, im) */
+    double *series;          /* NULL or rows * n_points doubles */
+    int64_t step;            /* step index of the next sample */
+    int64_t series_row;      /* series row of the next sample */
+} FdtdDftMonitor;
+
+/* Take one sample of a monitor (for per-call loops); advance mon->step and mon->series_row
+ * yourself. */
+int fdtd_monitor_sample(FdtdPlan *plan, const FdtdBuffers *buf, void *stream,
+                        const FdtdDftMonitor *mon);
+
+/* Deterministic FP64 sum over one plane of one component of a 3N field (field = E, H, S or
+ * any caller array of that layout): component 0..2, axis 0..2 normal to the plane, plane
+ * index along that axis. Two stages: per-block partial sums into scratch (scratch_len
+ * doubles, device; more gives more parallelism, the result does not depend on it beyond
+ * rounding of a fixed order), then one block folds them into *out (device double). */
+int fdtd_plane_sum(FdtdPlan *plan, const void *field, int32_t component, int32_t axis,
+                   int64_t plane, double *scratch, int32_t scratch_len, double *out, void *stream);
+
+/* Deterministic FP64 total field energy 1/2 sum(eps E^2 + mu H^2) (mu = 1 without mu; PEC
+ * cells hold none), with the same two-stage scheme into *out (device double). */
+int fdtd_energy(FdtdPlan *plan, const FdtdBuffers *buf, double *scratch, int32_t scratch_len,
+                double *out, void *stream);
+
 /* Run nsteps canonical steps (fdtd.py:162-175: E, F, point sources, H, G, S) on the stream
- * with no host round trip. src may be NULL. With the scratch buffers set (and no Bloch
+ * with no host round trip. src and mon may be NULL; mon is sampled after every step and its
+ * step / series_row advance by nsteps. With the scratch buffers set (and no Bloch
  * boundaries, at most 8 sources, no overlapping CPML faces) each step is one fused kernel;
  * oS is then written on the last step only. */
 int fdtd_run(FdtdPlan *plan, const FdtdBuffers *buf, void *stream, int32_t nsteps,
-             const FdtdPointSources *src);
+             const FdtdPointSources *src, FdtdDftMonitor *mon);
 
 #ifdef __cplusplus
 }

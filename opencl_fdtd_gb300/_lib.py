@@ -64,6 +64,11 @@ class FdtdPointSources(ctypes.Structure):
     _fields_ = [("n", c_i32), ("_pad", c_i32), ("index", c_vp), ("values", c_vp)]
 
 
+class FdtdDftMonitor(ctypes.Structure):
+    _fields_ = [("n_points", c_i32), ("n_freq", c_i32), ("index", c_vp), ("omega", c_vp),
+                ("accum", c_vp), ("series", c_vp), ("step", c_i64), ("series_row", c_i64)]
+
+
 # (name, restype, argtypes) of every entry point in include/fdtd_gb300.h
 _P = ctypes.POINTER
 SIGNATURES = [
@@ -80,7 +85,11 @@ SIGNATURES = [
     ("fdtd_update_f", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),
     ("fdtd_update_g", c_i32, [c_vp, _P(FdtdBuffers), c_vp]),
     ("fdtd_update_j", c_i32, [c_vp, _P(FdtdBuffers), c_vp, c_f64, c_f64, _P(c_i64)]),
-    ("fdtd_run", c_i32, [c_vp, _P(FdtdBuffers), c_vp, c_i32, _P(FdtdPointSources)]),
+    ("fdtd_monitor_sample", c_i32, [c_vp, _P(FdtdBuffers), c_vp, _P(FdtdDftMonitor)]),
+    ("fdtd_plane_sum", c_i32, [c_vp, c_vp, c_i32, c_i32, c_i64, c_vp, c_i32, c_vp, c_vp]),
+    ("fdtd_energy", c_i32, [c_vp, _P(FdtdBuffers), c_vp, c_i32, c_vp, c_vp]),
+    ("fdtd_run", c_i32, [c_vp, _P(FdtdBuffers), c_vp, c_i32, _P(FdtdPointSources),
+                         _P(FdtdDftMonitor)]),
 ]
 
 _LIB = None

@@ -15,6 +15,7 @@
 #include "yee_launch.h"
 #include "fdtd_plan.h"
 #include "fused.h"
+#include "monitors.h"
 
 using namespace fdtd;
 
@@ -235,6 +236,23 @@ int run_update_j(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, double c, d
     return check_cuda(launch_fieldsrc<R>(k, st), "update_J launch");
 }
 
+template <typename R>
+int run_dft(FdtdPlan *p, const void *field, cudaStream_t st, const FdtdDftMonitor *m, int64_t t)
+{
+    DftK<R> k;
+    k.field = (const R *)field;
+    k.index = m->index;
+    k.omega = m->omega;
+    k.accum = m->accum;
+    k.series = m->series;
+    k.npoint = m->n_points;
+    k.nfreq = m->n_freq;
+    k.step = m->step + t;
+    k.series_row = m->series_row + t;
+    k.dt = p->d.dt;
+    return check_cuda(launch_dft<R>(k, st), "DFT monitor launch");
+}
+
 // Add the sources whose x plane lies in [xbeg, xend) (all when the range is the grid).
 template <typename R>
 int run_point_sources(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st,
@@ -267,7 +285,7 @@ int run_point_sources(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st,
 // so results do not depend on the slab size.
 template <typename R>
 int run_slabs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
-              const FdtdPointSources *src)
+              const FdtdPointSources *src, const FdtdDftMonitor *mon)
 {
     const uint32_t sx = p->sx;
     const uint32_t W = p->slab ? p->slab : sx;
@@ -282,6 +300,7 @@ int run_slabs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
             if ((rc = run_update_h<R>(p, b, st, false))) return rc;
             if (bloch && (rc = run_update_h<R>(p, b, st, true))) return rc;
             if (poynt && (rc = run_update_s<R>(p, b, st))) return rc;
+            if (mon && (rc = run_dft<R>(p, b->E, st, mon, t))) return rc;
         }
         return FDTD_OK;
     }
@@ -302,6 +321,7 @@ int run_slabs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
             if ((rc = run_update_s<R>(p, b, st, sx - 1, sx))) return rc;
             if (sx > 1 && (rc = run_update_s<R>(p, b, st, 0, 1))) return rc;
         }
+        if (mon && (rc = run_dft<R>(p, b->E, st, mon, t))) return rc;
     }
     return FDTD_OK;
 }
@@ -319,7 +339,7 @@ uint32_t fused_cells_of(const FdtdPlan *p)
 // Fused multi-step path: one launch per step, reading A and writing B, then swapping.
 template <typename R>
 int run_fused(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
-              const FdtdPointSources *src)
+              const FdtdPointSources *src, const FdtdDftMonitor *mon)
 {
     FusedK<R> k;
     std::memset(&k, 0, sizeof(k));
@@ -399,6 +419,7 @@ int run_fused(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
         k.t = t;
         k.write_oS = poynt && t == nsteps - 1;
         int rc = check_cuda(launch_fused<R>(k, p->d.has_mu != 0, poynt, dxmode, st), "fused step launch");
+        if (!rc && mon) rc = run_dft<R>(p, E[o], st, mon, t);
         if (rc) return rc;
     }
     if (nsteps & 1) {
@@ -733,8 +754,94 @@ int fdtd_update_j(FdtdPlan *p, const FdtdBuffers *b, void *stream, double c, dou
                                   : run_update_j<float>(p, b, st, c, s, lo, n);
 }
 
+static int check_monitor(const FdtdPlan *p, const FdtdDftMonitor *m)
+{
+    if (!m) return FDTD_OK;
+    if (m->n_points < 0 || m->n_freq < 0) return fail(FDTD_ERR_INVALID, "monitor: negative sizes");
+    if (m->n_points && (!m->index || (m->n_freq && (!m->omega || !m->accum))))
+        return fail(FDTD_ERR_INVALID, "monitor: index, omega and accum are required");
+    if (m->n_points && !m->n_freq && !m->series)
+        return fail(FDTD_ERR_INVALID, "monitor: no frequency and no series");
+    if (m->n_freq == 0 && m->series) {
+        // series only: the kernel runs one thread per point with frequency slot 0 unused
+    }
+    return FDTD_OK;
+}
+
+int fdtd_monitor_sample(FdtdPlan *p, const FdtdBuffers *b, void *stream, const FdtdDftMonitor *m)
+{
+    int rc = check_common(p, b);
+    if (rc) return rc;
+    if (!m) return fail(FDTD_ERR_INVALID, "monitor is NULL");
+    if ((rc = check_monitor(p, m))) return rc;
+    if (!b->E) return fail(FDTD_ERR_INVALID, "monitor: E is required");
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == FDTD_F64 ? run_dft<double>(p, b->E, st, m, 0) : run_dft<float>(p, b->E, st, m, 0);
+}
+
+}  // extern "C"
+
+template <typename R>
+static int plane_sum_t(FdtdPlan *p, const void *field, int comp, int axis, int64_t plane,
+                       double *scratch, int nblk, double *out, cudaStream_t st)
+{
+    PlaneRedK<R> k;
+    k.src = (const R *)field + (uint64_t)comp * p->N;
+    k.partial = scratch;
+    const uint64_t sx = p->sx, sy = p->sy, sz = p->sz, syz = p->syz;
+    if (axis == 0) { k.base = plane * syz; k.stride_a = sz; k.stride_b = 1; k.inner = sz; k.ncell = syz; }
+    else if (axis == 1) { k.base = plane * sz; k.stride_a = syz; k.stride_b = 1; k.inner = sz; k.ncell = sx * sz; }
+    else { k.base = plane; k.stride_a = syz; k.stride_b = sz; k.inner = sy; k.ncell = sx * sy; }
+    return check_cuda(launch_plane_sum<R>(k, nblk, out, st), "plane sum launch");
+}
+
+extern "C" int fdtd_plane_sum(FdtdPlan *p, const void *field, int32_t comp, int32_t axis, int64_t plane,
+                   double *scratch, int32_t scratch_len, double *out, void *stream)
+{
+    if (!p) return fail(FDTD_ERR_INVALID, "plan is NULL");
+    if (!field || !scratch || !out) return fail(FDTD_ERR_INVALID, "plane sum: NULL pointer");
+    if (comp < 0 || comp > 2 || axis < 0 || axis > 2) return fail(FDTD_ERR_INVALID, "plane sum: component and axis must be 0..2");
+    const int64_t s = axis == 0 ? p->sx : axis == 1 ? p->sy : p->sz;
+    if (plane < 0 || plane >= s) return fail(FDTD_ERR_INVALID, "plane sum: plane index out of range");
+    if (scratch_len < 1) return fail(FDTD_ERR_INVALID, "plane sum: scratch_len must be >= 1");
+    const int nblk = scratch_len < 1024 ? scratch_len : 1024;
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == FDTD_F64 ? plane_sum_t<double>(p, field, comp, axis, plane, scratch, nblk, out, st)
+                                  : plane_sum_t<float>(p, field, comp, axis, plane, scratch, nblk, out, st);
+}
+
+template <typename R>
+static int energy_t(FdtdPlan *p, const FdtdBuffers *b, double *scratch, int nblk, double *out,
+                    cudaStream_t st)
+{
+    EnergyK<R> k;
+    k.E = (const R *)b->E;
+    k.H = (const R *)b->H;
+    k.eps = (const R *)b->eps;
+    k.mu = p->d.has_mu ? (const R *)b->mu : nullptr;
+    k.partial = scratch;
+    k.n = 3 * p->N;
+    return check_cuda(launch_energy<R>(k, nblk, out, st), "energy launch");
+}
+
+extern "C" {
+
+int fdtd_energy(FdtdPlan *p, const FdtdBuffers *b, double *scratch, int32_t scratch_len,
+                double *out, void *stream)
+{
+    int rc = check_common(p, b);
+    if (rc) return rc;
+    if (!b->E || !b->H || !b->eps) return fail(FDTD_ERR_INVALID, "energy: E, H and eps are required");
+    if (p->d.has_mu && !b->mu) return fail(FDTD_ERR_INVALID, "energy: mu is required");
+    if (!scratch || !out || scratch_len < 1) return fail(FDTD_ERR_INVALID, "energy: scratch and out are required");
+    const int nblk = scratch_len < 1024 ? scratch_len : 1024;
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == FDTD_F64 ? energy_t<double>(p, b, scratch, nblk, out, st)
+                                  : energy_t<float>(p, b, scratch, nblk, out, st);
+}
+
 int fdtd_run(FdtdPlan *p, const FdtdBuffers *b, void *stream, int32_t nsteps,
-             const FdtdPointSources *src)
+             const FdtdPointSources *src, FdtdDftMonitor *mon)
 {
     int rc = check_common(p, b);
     if (rc) return rc;
@@ -746,17 +853,22 @@ int fdtd_run(FdtdPlan *p, const FdtdBuffers *b, void *stream, int32_t nsteps,
     for (int s = 0; src && s < src->n; ++s)
         if (src->index[s] < 0 || (uint64_t)src->index[s] >= 3 * p->N)
             return fail(FDTD_ERR_INVALID, "fdtd_run: point source index out of range");
+    if ((rc = check_monitor(p, mon))) return rc;
     const bool f64 = p->d.dtype == FDTD_F64;
     if (fused_eligible(p, b, src)) {
         if ((rc = check_psi(p, b->psi_e, "fdtd_run")) || (rc = check_psi(p, b->psi_h, "fdtd_run")))
             return rc;
         cudaStream_t st = (cudaStream_t)stream;
-        return f64 ? run_fused<double>(p, b, st, nsteps, src) : run_fused<float>(p, b, st, nsteps, src);
+        rc = f64 ? run_fused<double>(p, b, st, nsteps, src, mon) : run_fused<float>(p, b, st, nsteps, src, mon);
+        if (!rc && mon) { mon->step += nsteps; mon->series_row += nsteps; }
+        return rc;
     }
     // validate once with the per-update entry points' checks, then run the slab schedule
     if ((rc = check_run_buffers(p, b))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    return f64 ? run_slabs<double>(p, b, st, nsteps, src) : run_slabs<float>(p, b, st, nsteps, src);
+    rc = f64 ? run_slabs<double>(p, b, st, nsteps, src, mon) : run_slabs<float>(p, b, st, nsteps, src, mon);
+    if (!rc && mon) { mon->step += nsteps; mon->series_row += nsteps; }
+    return rc;
 }
 
 }  // extern "C"

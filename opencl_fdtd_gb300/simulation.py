@@ -456,7 +456,8 @@ class Simulation:
     # ------------------------------------------------------------------------------------
     # additions beyond the reference
     # ------------------------------------------------------------------------------------
-    def run(self, nsteps: int, point_sources=None, wait_for=None, fused: bool = False) -> Event:
+    def run(self, nsteps: int, point_sources=None, wait_for=None, fused: bool = False,
+            monitor=None) -> Event:
         """Advance ``nsteps`` canonical steps (E, F, point sources, H, G, S) in one call.
 
         ``point_sources`` is a list of (flat_index, values) pairs: after the E update of step
@@ -495,13 +496,59 @@ class Simulation:
             self._ensure_scratch()
         bufs = self._buffers()
         self._attach_scratch(use_fused)
+        mon = monitor.struct(nsteps) if monitor is not None else None
         _lib.check(self._lib.fdtd_run(self._plan, ctypes.byref(bufs),
                                       ctypes.c_void_p(stream.cuda_stream), nsteps,
-                                      ctypes.byref(src) if src is not None else None))
+                                      ctypes.byref(src) if src is not None else None,
+                                      ctypes.byref(mon) if mon is not None else None))
+        if monitor is not None:
+            monitor.samples += nsteps
         for t in keep:
             t.record_stream(stream)
         self.steps_run += nsteps
         return Event(stream)
+
+    # ---- FP64 monitors --------------------------------------------------------------------
+    def dft_monitor(self, points, omegas=(), record: bool = True, t0: int = None):
+        """A DftMonitor on this simulation (pass it to run(monitor=...) or call sample())."""
+        from .monitors import DftMonitor
+        return DftMonitor(self, points, omegas, record=record,
+                          t0=self.steps_run if t0 is None else t0)
+
+    def _reduction_buffers(self):
+        if getattr(self, "_red", None) is None:
+            self._red = (torch.empty(1024, dtype=torch.float64, device=self.device),
+                         torch.empty(1, dtype=torch.float64, device=self.device))
+        return self._red
+
+    def plane_sum(self, field: str, component: int, axis, index: int) -> float:
+        """FP64 sum of one component of E, H or S over the plane ``index`` normal to ``axis``
+        (a Poynting-flux integral for field 'S' and component == axis, in cell units)."""
+        a = "xyz".index(axis) if isinstance(axis, str) else int(axis)
+        t = getattr(self, field)
+        self._check_field(t, field, 3 * self.N)
+        scratch, out = self._reduction_buffers()
+        _lib.check(self._lib.fdtd_plane_sum(self._plan, t.data_ptr(), int(component), a, int(index),
+                                            scratch.data_ptr(), scratch.numel(), out.data_ptr(),
+                                            ctypes.c_void_p(self.queue.cuda_stream)))
+        self.queue.synchronize()
+        return float(out.item())
+
+    def flux(self, axis, index: int) -> float:
+        """Poynting flux through plane ``index`` normal to ``axis``: sum of S_axis there."""
+        if not self.do_poynting:
+            raise Exception("flux needs do_poynting=True")
+        a = "xyz".index(axis) if isinstance(axis, str) else int(axis)
+        return self.plane_sum("S", a, a, index)
+
+    def energy(self) -> float:
+        """FP64 total field energy 1/2 sum(eps E^2 + mu H^2) (PEC cells excluded)."""
+        scratch, out = self._reduction_buffers()
+        _lib.check(self._lib.fdtd_energy(self._plan, ctypes.byref(self._buffers()), scratch.data_ptr(),
+                                         scratch.numel(), out.data_ptr(),
+                                         ctypes.c_void_p(self.queue.cuda_stream)))
+        self.queue.synchronize()
+        return float(out.item())
 
     def slab_planes(self) -> int:
         """x planes per slab of run()'s per-update schedule (whole grid when 0)."""
