@@ -191,6 +191,19 @@ int fdtd_monitor_sample(FdtdPlan *plan, const FdtdBuffers *buf, void *stream,
 int fdtd_plane_sum(FdtdPlan *plan, const void *field, int32_t component, int32_t axis,
                    int64_t plane, double *scratch, int32_t scratch_len, double *out, void *stream);
 
+/* fdtd_plane_sum without allocation — no counterpart in the reference, which has no
+ * monitors. For callers that must not allocate device memory between steps (a host driver
+ * that has given the device memory to its own pool, or a callback between queued steps where
+ * cudaMalloc/cudaFree would synchronize the device): the nblocks per-block partial sums go to
+ * a static device array of this library (at most 1024 doubles, 8 KB, held on every GPU that
+ * loads the library until exit) instead of caller scratch. nblocks must be in [1, 1024];
+ * larger values are rejected with FDTD_ERR_INVALID. The first call on a device resolves the
+ * array's device address (cudaGetSymbolAddress), so make it before any stream capture. Every
+ * call writes the partials it reads (nothing needs clearing; the array keeps the last call's
+ * values); calls share the array, so calls whose kernels overlap on the GPU race. */
+int fdtd_plane_sum_noalloc(FdtdPlan *plan, const void *field, int32_t component, int32_t axis,
+                           int64_t plane, int32_t nblocks, double *out, void *stream);
+
 /* Deterministic FP64 total field energy 1/2 sum(eps E^2 + mu H^2) (mu = 1 without mu; PEC
  * cells hold none), with the same two-stage scheme into *out (device double). */
 int fdtd_energy(FdtdPlan *plan, const FdtdBuffers *buf, double *scratch, int32_t scratch_len,

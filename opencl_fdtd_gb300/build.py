@@ -32,6 +32,7 @@ UNITS = {
     "yee_kernels.cu": ["--fmad=false"],
     "step_fused.cu": ["--fmad=false"],
     "monitors.cu": [],
+    "noalloc.cu": [],
     "fdtd_abi.cu": [],
 }
 
