@@ -248,14 +248,16 @@ def time_dropin(sim, lib, wave_dev, ind, K, W, poynting, world):
             step(t)
         torch.cuda.synchronize()
         if world > 1:
-            torch.distributed.barrier()
+            from opencl_fdtd_gb300 import replicas
+            replicas.barrier()
         evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(K)]
         torch.cuda.synchronize()
         for t in range(K):
             step(W + t, evs[t])
         torch.cuda.synchronize()
         if world > 1:
-            torch.distributed.barrier()
+            from opencl_fdtd_gb300 import replicas
+            replicas.barrier()
     total = evs[0][0].elapsed_time(evs[-1][4])
     per = {"k_bulk_e": statistics.mean(evs[t][0].elapsed_time(evs[t][1]) for t in range(K)),
            "k_bulk_h": statistics.mean(evs[t][2].elapsed_time(evs[t][3]) for t in range(K))}
@@ -283,7 +285,8 @@ def time_run(sim, lib, wave_dev, ind, K, W, world, fused: bool):
         _lib.check(lib.fdtd_run(sim._plan, ctypes.byref(bufs), st, W, ctypes.byref(warm), None))
         torch.cuda.synchronize()
         if world > 1:
-            torch.distributed.barrier()
+            from opencl_fdtd_gb300 import replicas
+            replicas.barrier()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -291,7 +294,8 @@ def time_run(sim, lib, wave_dev, ind, K, W, world, fused: bool):
         e1.record(stream)
         torch.cuda.synchronize()
         if world > 1:
-            torch.distributed.barrier()
+            from opencl_fdtd_gb300 import replicas
+            replicas.barrier()
     return e0.elapsed_time(e1)
 
 
@@ -342,12 +346,10 @@ def main():
         res["fused"] = time_run(sim, lib, wave_dev, ind, K, W, world, fused=True)
     clock = clocks.stop()
 
+    from opencl_fdtd_gb300 import replicas
+
     def allmax(v):
-        if world == 1:
-            return v
-        tt = torch.tensor([v], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        return float(tt.item())
+        return replicas.max_over_ranks(v, device="cuda")
 
     peak, peak_kind = peak_hbm()
     per_launch, step_bytes = algorithmic_bytes(N, fc, elem, poynting)

@@ -595,6 +595,19 @@ class Simulation:
                 v.copy_(sv)
         self.steps_run = int(st.get("steps_run", 0))
 
+    def save_snapshot(self, path, grid=None):
+        """Write {'grid', 'E', 'H'[, 'S']} as opencl_fdtd's driver does (fdtd.py:181-191)."""
+        from .snapshot import save_snapshot
+        save_snapshot(self, path, grid)
+
+    def save_checkpoint(self, path):
+        from .snapshot import save_checkpoint
+        save_checkpoint(self, path)
+
+    def load_checkpoint(self, path):
+        from .snapshot import load_checkpoint
+        load_checkpoint(self, path)
+
     def close(self):
         if self._plan:
             self._lib.fdtd_plan_destroy(self._plan)

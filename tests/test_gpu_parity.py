@@ -151,3 +151,25 @@ def test_constructor_errors():
         Simulation([one] * 3, [{"axis": "x", "polarity": "n"}, {"axis": "x", "polarity": "n"}])
     with pytest.raises(Exception, match="Unsupported type"):
         Simulation([one] * 3, [], float_type=numpy.float16)
+
+
+def test_snapshot_and_checkpoint_resume(tmp_path):
+    """The driver's snapshot dict, and a checkpoint that resumes bit for bit."""
+    from opencl_fdtd_gb300 import snapshot
+    kw, loop = cases.build("pml_mixed")
+    import copy
+    a = _gpu(**copy.deepcopy(kw))
+    a.run(10)
+    a.save_snapshot(tmp_path / "snap.xz")
+    d = snapshot.load_snapshot(tmp_path / "snap.xz")
+    shape = kw["epsilon"][0].shape
+    assert d["E"].shape == (3, *shape) and numpy.array_equal(d["E"].reshape(-1), a.get("E"))
+    assert numpy.array_equal(d["S"].reshape(-1), a.get("S"))
+    a.save_checkpoint(tmp_path / "ck.pt")
+    a.run(7)
+    b = _gpu(**copy.deepcopy(kw))
+    b.load_checkpoint(tmp_path / "ck.pt")
+    b.run(7)
+    for k in ("E", "H", "S"):
+        assert torch.equal(getattr(a, k), getattr(b, k)), k
+    assert b.steps_run == 17
