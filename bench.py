@@ -58,9 +58,11 @@ def parse():
     ap.add_argument("--fused-cells", type=int, default=0)
     ap.add_argument("--fused-xchunk", type=int, default=0)
     ap.add_argument("--slab", type=int, default=-1, help="x planes per L2 slab (-1: plan default)")
-    ap.add_argument("--path", choices=["fused", "slab", "dropin", "default", "all"], default="default",
-                    help="default = per-call loop (per-kernel timing) + Simulation.run; "
-                         "slab = Simulation.run over the per-update kernels; fused = the opt-in fused step")
+    ap.add_argument("--hs-xchunk", type=int, default=0)
+    ap.add_argument("--hs-prefetch", type=int, default=-1)
+    ap.add_argument("--path", choices=["fused", "slab", "hs", "dropin", "default", "all"], default="default",
+                    help="default = per-call loop (per-kernel timing) + Simulation.run (hs path); "
+                         "slab = run over the per-update kernels; fused = the opt-in fused step")
     return ap.parse_args()
 
 
@@ -266,16 +268,16 @@ def time_dropin(sim, lib, wave_dev, ind, K, W, poynting, world):
     return total, per
 
 
-def time_run(sim, lib, wave_dev, ind, K, W, world, fused: bool):
-    """K steps in one fdtd_run call bracketed by CUDA events: fused (one kernel per step,
-    scratch buffers attached) or the per-update kernels over L2-resident slabs."""
+def time_run(sim, lib, wave_dev, ind, K, W, world, mode):
+    """K steps in one fdtd_run call bracketed by CUDA events. mode: 'hs' (E in place, H and S
+    in one launch), 'fused' (one kernel per step) or None (the per-update kernels)."""
     import torch
     from opencl_fdtd_gb300 import _lib
     stream = sim.queue
-    if fused:
-        sim._ensure_scratch()
+    if mode:
+        sim._ensure_scratch(mode)
     bufs = sim._buffers()
-    sim._attach_scratch(fused)
+    sim._attach_scratch(mode)
     st = ctypes.c_void_p(stream.cuda_stream)
     idx = (ctypes.c_int64 * 1)(ind)
     esz = wave_dev.element_size()
@@ -323,6 +325,10 @@ def main():
         sim.tune(fused_xchunk=args.fused_xchunk)
     if args.slab >= 0:
         sim.tune(slab=args.slab)
+    if args.hs_xchunk:
+        sim.tune(hs_xchunk=args.hs_xchunk)
+    if args.hs_prefetch >= 0:
+        sim.tune(hs_prefetch=bool(args.hs_prefetch))
     N = int(numpy.prod(wl["shape"]))
     fc = workloads.face_cells(wl["shape"], kw["pmls"])
     poynting = kw.get("do_poynting", True)
@@ -339,11 +345,13 @@ def main():
     res = {}
     if args.path in ("dropin", "default", "all"):
         res["dropin"] = time_dropin(sim, lib, wave_dev, ind, K, W, poynting, world)
-    if args.path in ("slab", "default", "all"):
-        res["slab"] = time_run(sim, lib, wave_dev, ind, K, W, world, fused=False)
+    if args.path in ("hs", "default", "all") and poynting:
+        res["hs"] = time_run(sim, lib, wave_dev, ind, K, W, world, "hs")
+    if args.path in ("slab", "all"):
+        res["slab"] = time_run(sim, lib, wave_dev, ind, K, W, world, None)
         sim.tune(slab=0)
     if args.path in ("fused", "all"):
-        res["fused"] = time_run(sim, lib, wave_dev, ind, K, W, world, fused=True)
+        res["fused"] = time_run(sim, lib, wave_dev, ind, K, W, world, "fused")
     clock = clocks.stop()
 
     from opencl_fdtd_gb300 import replicas
@@ -369,17 +377,20 @@ def main():
                          "mean_launch_ms": round(per[dom], 5),
                          "per_kernel_ms": {k: round(v, 5) for k, v in per.items()}}}
     compulsory = N * (18 if poynting else 15) * elem + fc * 8 * elem
-    for name in ("fused", "slab"):
+    for name in ("fused", "slab", "hs"):
         if name not in res:
             continue
         total = allmax(res[name])
         ms = total / K
         ach = step_bytes / (ms * 1e-3) / 1e9
         nslab = (wl["shape"][0] + sim.slab_planes() - 1) // sim.slab_planes()
-        launches = K if name == "fused" else K * ((3 if poynting else 2) * nslab + (3 if poynting else 1) + 1)
+        launches = {"fused": K, "hs": 3 * K,
+                    "slab": K * ((3 if poynting else 2) * nslab + (3 if poynting else 1) + 1)}[name]
+        kname = {"fused": "k_fused_step", "hs": "step (k_bulk_e + k_bulk_hs)",
+                 "slab": "step (k_bulk_e/h/s over L2 slabs)"}[name]
         out_paths[name] = {
             "ms_per_step": ms, "value": world * N * K / (total * 1e-3) / 1e6, "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "kernel": "k_fused_step" if name == "fused" else "step (k_bulk_e/h/s over L2 slabs)",
+            "roofline": {"bound": "hbm", "kernel": kname,
                          "achieved": round(ach, 1),
                          "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4),
                          "peak_source": peak_kind, "traffic": traffic.get(name),
@@ -388,7 +399,7 @@ def main():
                          "compulsory_bytes_per_step": compulsory,
                          "compulsory_frac": round(compulsory / (ms * 1e-3) / 1e9 / peak, 4),
                          "mean_step_ms": round(ms, 5)}}
-    cands = [n for n in ("fused", "slab") if n in out_paths]
+    cands = [n for n in ("fused", "slab", "hs") if n in out_paths]
     head = min(cands, key=lambda n: out_paths[n]["ms_per_step"]) if cands else "dropin"
     hp = out_paths[head]
     step_gbs = step_bytes / (hp["ms_per_step"] * 1e-3) / 1e9
@@ -396,7 +407,7 @@ def main():
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(sim, wl, args.e2e_steps, world, run_api=(head != "dropin"),
-                      fused=(head == "fused"))
+                      path={"fused": "fused", "hs": "hs", "slab": "plain"}.get(head, "auto"))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -410,8 +421,9 @@ def main():
             "data": "synthetic (seeded L3 cavity geometry and source)",
             "config": {"workload": wl["describe"], "grid": list(wl["shape"]), "cells": N,
                        "cpml_face_cells": fc,
-                       "path": {"fused": "Simulation.run: one fused E+source+H+S kernel per step",
-                                "slab": "Simulation.run: E, point source, H, S update kernels per step (whole grid)",
+                       "path": {"fused": "Simulation.run(path='fused'): one fused E+source+H+S kernel per step",
+                                "hs": "Simulation.run: E in place, point source, H+S in one launch (H ping-pong)",
+                                "slab": "Simulation.run(path='plain'): E, point source, H, S update kernels",
                                 "dropin": "per-call update_E / source add / update_H / update_S"}[head],
                        "l2": "inputs (~%.0f MB of fields) larger than the 129 MB L2; no flush"
                              % (sim.E.numel() * elem * (6 if poynting else 3) / 1e6),
@@ -433,7 +445,7 @@ def main():
         torch.distributed.destroy_process_group()
 
 
-def run_e2e(sim, wl, steps: int, world: int, run_api: bool = False, fused: bool = False):
+def run_e2e(sim, wl, steps: int, world: int, run_api: bool = False, path: str = "auto"):
     """End to end through the public API with host buffers.
 
     fused: Simulation.run() in calls of 10 steps, each given its 10 source samples from host
@@ -446,12 +458,12 @@ def run_e2e(sim, wl, steps: int, world: int, run_api: bool = False, fused: bool 
         chunk = 10
         host = numpy.array([wl["wave"](t) for t in range(steps + 2 * chunk)], dtype=numpy.float64)
         probe = numpy.empty(steps // chunk + 2, numpy.float32)
-        sim.run(chunk, point_sources=[(ind, host[:chunk])], fused=fused).wait()
+        sim.run(chunk, point_sources=[(ind, host[:chunk])], path=path).wait()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         n = 0
         for c in range(steps // chunk):
-            sim.run(chunk, point_sources=[(ind, host[c * chunk:(c + 1) * chunk])], fused=fused)
+            sim.run(chunk, point_sources=[(ind, host[c * chunk:(c + 1) * chunk])], path=path)
             probe[c] = float(sim.E[ind:ind + 1].cpu())
             n += chunk
         torch.cuda.synchronize()

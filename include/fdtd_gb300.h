@@ -122,11 +122,16 @@ int fdtd_plan_destroy(FdtdPlan *plan);
  *   SLAB          x planes per L2-resident slab of fdtd_run's per-update schedule
  *                 (default 0 = whole grid)
  *   FUSED_CELLS   plane cells one block of the fused step owns (0 = the maximum, 768 - 2*sz)
- *   FUSED_XCHUNK  x planes one block of the fused step marches (default 16) */
+ *   FUSED_XCHUNK  x planes one block of the fused step marches (default 16)
+ *   HS_XCHUNK     x planes one block of the H+S kernel of fdtd_run marches (default 16)
+ *   HS_PREFETCH   1: the H+S kernel loads the next plane ahead (one block per SM); 0: not
+ *                 (two blocks per SM, the default) */
 #define FDTD_TUNE_XCHUNK 1
 #define FDTD_TUNE_SLAB 2
 #define FDTD_TUNE_FUSED_CELLS 3
 #define FDTD_TUNE_FUSED_XCHUNK 4
+#define FDTD_TUNE_HS_XCHUNK 5
+#define FDTD_TUNE_HS_PREFETCH 6
 int fdtd_plan_tune(FdtdPlan *plan, int32_t key, int32_t value);
 /* Current value of a tuning key. */
 int fdtd_plan_get(const FdtdPlan *plan, int32_t key, int32_t *value);

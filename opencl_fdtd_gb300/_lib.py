@@ -27,6 +27,8 @@ FDTD_TUNE_XCHUNK = 1
 FDTD_TUNE_SLAB = 2
 FDTD_TUNE_FUSED_CELLS = 3
 FDTD_TUNE_FUSED_XCHUNK = 4
+FDTD_TUNE_HS_XCHUNK = 5
+FDTD_TUNE_HS_PREFETCH = 6
 
 
 class FdtdPmlDesc(ctypes.Structure):

@@ -31,6 +31,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "yee_kernels.cu": ["--fmad=false"],
     "step_fused.cu": ["--fmad=false"],
+    "hs_fused.cu": ["--fmad=false"],
     "monitors.cu": [],
     "noalloc.cu": [],
     "fdtd_abi.cu": [],

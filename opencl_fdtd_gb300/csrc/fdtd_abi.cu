@@ -16,6 +16,7 @@
 #include "fdtd_plan.h"
 #include "fused.h"
 #include "monitors.h"
+#include "hs_fused.h"
 
 using namespace fdtd;
 
@@ -278,6 +279,83 @@ int run_point_sources(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st,
     return check_cuda(launch_point_sources<R>(k, st), "point source launch");
 }
 
+// Multi-step path with the H+S kernel: update_E in place, point sources, then H and S in one
+// launch that reads H (and the H-side psi) from one copy and writes the other; the copies
+// swap every step and the state is brought home after an odd number of steps.
+template <typename R>
+int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
+           const FdtdPointSources *src, const FdtdDftMonitor *mon)
+{
+    HSK<R> k;
+    std::memset(&k, 0, sizeof(k));
+    k.sx = p->sx;
+    k.sy = p->sy;
+    k.sz = p->sz;
+    k.syz = p->syz;
+    k.N = p->N;
+    k.dt = (R)p->d.dt;
+    k.inv_d = (R)(1.0 / p->d.dx);
+    k.sf = (R)((double)k.dt * 0.125);
+    for (int r = 0; r < 3; ++r) k.inv_de[r] = p->d.uniform ? nullptr : (const R *)b->inv_de[r];
+    const int dxmode = !p->d.uniform ? 2 : ((R)(1.0 / p->d.dx) == R(1) ? 0 : 1);
+    k.cm = p->d.has_mu ? (const R *)b->cm : nullptr;
+    k.S = (R *)b->S;
+    k.oS = (R *)b->oS;
+    k.dsz = FastDiv::make(p->sz);
+    k.rows = (uint32_t)HS_THREADS / p->sz - 1u;
+    k.xchunk = p->hs_xchunk;
+    int fidx[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
+    for (int f = 0; f < p->d.n_pml; ++f) {
+        const FdtdPmlDesc &pd = p->d.pml[f];
+        const uint32_t sa = pd.axis == 0 ? p->sx : pd.axis == 1 ? p->sy : p->sz;
+        if (pd.polarity == 1 && (uint32_t)pd.thickness > sa) continue;
+        HSAxis<R> &a = k.ax[pd.axis];
+        if (pd.polarity == 0) a.Tn = pd.thickness;
+        else a.Tp = pd.thickness;
+        for (int c = 0; c < 3; ++c) a.tab[pd.polarity][c] = (const R *)p->tab[f][3 + c];
+        fidx[pd.axis][pd.polarity] = f;
+    }
+    FdtdBuffers bb = *b;
+    void *H[2] = {b->H, b->H2};
+    int rc;
+    for (int t = 0; t < nsteps; ++t) {
+        const int a = t & 1, o = a ^ 1;
+        bb.H = H[a];
+        if ((rc = run_update_e<R>(p, &bb, st, false))) return rc;
+        if (src && src->n > 0 && (rc = run_point_sources<R>(p, &bb, st, src, t))) return rc;
+        k.E = (const R *)b->E;
+        k.HA = (const R *)H[a];
+        k.HB = (R *)H[o];
+        for (int r = 0; r < 3; ++r)
+            for (int side = 0; side < 2; ++side) {
+                const int f = fidx[r][side];
+                if (f < 0) continue;
+                void *const *pa = a ? b->psi_h2[f] : b->psi_h[f];
+                void *const *po = o ? b->psi_h2[f] : b->psi_h[f];
+                for (int c = 0; c < 2; ++c) {
+                    k.ax[r].A[side][c] = (const R *)pa[c];
+                    k.ax[r].B[side][c] = (R *)po[c];
+                }
+            }
+        k.write_oS = t == nsteps - 1;
+        if ((rc = check_cuda(launch_hs<R>(k, p->d.has_mu != 0, dxmode, p->hs_prefetch != 0, st), "H+S launch"))) return rc;
+        if (mon && (rc = run_dft<R>(p, b->E, st, mon, t))) return rc;
+    }
+    if (nsteps & 1) {
+        const size_t fb = 3 * (size_t)p->N * p->elem;
+        rc = check_cuda(cudaMemcpyAsync(b->H, b->H2, fb, cudaMemcpyDeviceToDevice, st), "copy H");
+        for (int f = 0; !rc && f < p->d.n_pml; ++f) {
+            const FdtdPmlDesc &pd = p->d.pml[f];
+            const size_t cells = (size_t)p->N / (pd.axis == 0 ? p->sx : pd.axis == 1 ? p->sy : p->sz);
+            const size_t pb = cells * (size_t)pd.thickness * p->elem;
+            for (int c = 0; !rc && c < 2 && pb; ++c)
+                rc = check_cuda(cudaMemcpyAsync(b->psi_h[f][c], b->psi_h2[f][c], pb, cudaMemcpyDeviceToDevice, st), "copy psi_h");
+        }
+        if (rc) return rc;
+    }
+    return FDTD_OK;
+}
+
 // Per-update kernels over x slabs small enough to stay resident in L2: E on slab s, then H
 // one plane behind (H at x needs E_new at x+1; E at x needs H_old at x-1), then S one plane
 // behind H. Within a step each update's reads of the previous update's output hit L2 while
@@ -522,6 +600,18 @@ bool fused_eligible(const FdtdPlan *p, const FdtdBuffers *b, const FdtdPointSour
     return smem <= 200 * 1024;
 }
 
+// The H+S path: Poynting on, no Bloch boundaries, CPML faces of one axis disjoint, dt/eps
+// (and dt/mu) caches and the H scratch copies present, and a z row that fits a block.
+bool hs_eligible(const FdtdPlan *p, const FdtdBuffers *b)
+{
+    if (!p->d.do_poynting || p->d.n_bloch || !faces_disjoint(p)) return false;
+    if (!b->ce || (p->d.has_mu && !b->cm) || !b->H2 || !b->S || !b->oS) return false;
+    if (2 * p->sz > (uint32_t)HS_THREADS) return false;   // at least one own row plus the halo row
+    for (int f = 0; f < p->d.n_pml; ++f)
+        if (p->d.pml[f].thickness > 0 && (!b->psi_h2[f][0] || !b->psi_h2[f][1])) return false;
+    return true;
+}
+
 int check_inv(const FdtdPlan *p, const void *const inv[3], const char *what)
 {
     if (p->d.uniform) return FDTD_OK;
@@ -560,6 +650,8 @@ int fdtd_plan_create(const FdtdDesc *desc, FdtdPlan **out)
     // step against 0.43-0.86 ms for 48- to 8-plane slabs), so slabs are opt-in.
     p->slab = 0;
     p->fused_cells = 0;
+    p->hs_xchunk = 16;
+    p->hs_prefetch = 0;
     p->fused_xchunk = 16;
     cudaGetDevice(&p->device);
     size_t total = 0;
@@ -624,6 +716,14 @@ int fdtd_plan_tune(FdtdPlan *p, int32_t key, int32_t value)
         if (value < 1 || value > 4096) return fail(FDTD_ERR_INVALID, "fused_xchunk must be in [1, 4096]");
         p->fused_xchunk = (uint32_t)value;
         return FDTD_OK;
+    case FDTD_TUNE_HS_XCHUNK:
+        if (value < 1 || value > 4096) return fail(FDTD_ERR_INVALID, "hs_xchunk must be in [1, 4096]");
+        p->hs_xchunk = (uint32_t)value;
+        return FDTD_OK;
+    case FDTD_TUNE_HS_PREFETCH:
+        if (value != 0 && value != 1) return fail(FDTD_ERR_INVALID, "hs_prefetch must be 0 or 1");
+        p->hs_prefetch = value;
+        return FDTD_OK;
     default:
         return fail(FDTD_ERR_INVALID, "unknown tuning key");
     }
@@ -637,6 +737,8 @@ int fdtd_plan_get(const FdtdPlan *p, int32_t key, int32_t *value)
     case FDTD_TUNE_SLAB: *value = (int32_t)p->slab; return FDTD_OK;
     case FDTD_TUNE_FUSED_CELLS: *value = (int32_t)p->fused_cells; return FDTD_OK;
     case FDTD_TUNE_FUSED_XCHUNK: *value = (int32_t)p->fused_xchunk; return FDTD_OK;
+    case FDTD_TUNE_HS_XCHUNK: *value = (int32_t)p->hs_xchunk; return FDTD_OK;
+    case FDTD_TUNE_HS_PREFETCH: *value = p->hs_prefetch; return FDTD_OK;
     default: return fail(FDTD_ERR_INVALID, "unknown tuning key");
     }
 }
@@ -855,6 +957,13 @@ int fdtd_run(FdtdPlan *p, const FdtdBuffers *b, void *stream, int32_t nsteps,
             return fail(FDTD_ERR_INVALID, "fdtd_run: point source index out of range");
     if ((rc = check_monitor(p, mon))) return rc;
     const bool f64 = p->d.dtype == FDTD_F64;
+    if (!b->E2 && hs_eligible(p, b)) {
+        if ((rc = check_run_buffers(p, b))) return rc;
+        cudaStream_t st = (cudaStream_t)stream;
+        rc = f64 ? run_hs<double>(p, b, st, nsteps, src, mon) : run_hs<float>(p, b, st, nsteps, src, mon);
+        if (!rc && mon) { mon->step += nsteps; mon->series_row += nsteps; }
+        return rc;
+    }
     if (fused_eligible(p, b, src)) {
         if ((rc = check_psi(p, b->psi_e, "fdtd_run")) || (rc = check_psi(p, b->psi_h, "fdtd_run")))
             return rc;

@@ -16,6 +16,8 @@ struct FdtdPlan {
     uint32_t slab;              // x planes per L2-resident slab in fdtd_run (0: whole grid)
     uint32_t fused_cells;       // plane cells one block of the fused step owns
     uint32_t fused_xchunk;      // x planes one block of the fused step marches
+    uint32_t hs_xchunk;         // x planes one block of the H+S kernel marches
+    int32_t hs_prefetch;        // H+S kernel issues the next plane's loads early
     void *coef = nullptr;       // device copy of every face's six coefficient tables
     const void *tab[6][6];      // per face: p0e p1e p2e p0h p1h p2h (device pointers)
 };

@@ -1,0 +1,42 @@
+// Arguments and launcher of the H+S kernel (hs_fused.cu).
+#pragma once
+
+#include "yee_common.cuh"
+
+namespace fdtd {
+
+// threads of an H+S block: whole z rows, the block's own rows plus one halo row,
+// rows = HS_THREADS / sz - 1
+constexpr int HS_THREADS = 512;
+
+// H-side CPML faces of one axis: tables [n/p][p0,p1,p2], old (A) and new (B) psi [n/p][u/v].
+// Tp = 0 when the 'p' face never applies.
+template <typename R>
+struct HSAxis {
+    int32_t Tn, Tp;
+    const R *tab[2][3];
+    const R *A[2][2];
+    R *B[2][2];
+};
+
+template <typename R>
+struct HSK {
+    const R *E;            // E after this step's update and sources (read-only here)
+    const R *HA;           // H before the update
+    R *HB;                 // H after the update
+    R *S, *oS;             // S every launch; oS only when write_oS
+    const R *cm;           // dt/mu, NULL without mu
+    uint32_t sx, sy, sz, syz;
+    uint64_t N;
+    R dt, inv_d, sf;
+    const R *inv_de[3];
+    HSAxis<R> ax[3];
+    FastDiv dsz;
+    uint32_t rows, xchunk;
+    int32_t write_oS, _pad;
+};
+
+template <typename R>
+cudaError_t launch_hs(const HSK<R> &k, bool mu, int dxmode, bool prefetch, cudaStream_t st);
+
+}  // namespace fdtd

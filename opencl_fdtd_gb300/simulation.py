@@ -389,36 +389,42 @@ class Simulation:
         if self._cm is not None:
             b.cm = self._cm.data_ptr()
         self._buf = b
-        self._attach_scratch()
+        self._attach_scratch(None)
         self._buf_key = key
         self._prepare((self.eps._version, None if self.mu is None else self.mu._version))
         return b
 
-    def _attach_scratch(self, on: bool = True):
+    def _attach_scratch(self, mode=None):
+        """Point the C buffers at the second copies a run path uses: 'fused' (E, H and both
+        CPML sides), 'hs' (H and the H-side CPML arrays) or None (no second copies)."""
         b = self._buf
-        if on and self._scratch is not None:
-            E2, H2, pe2, ph2 = self._scratch
-            b.E2, b.H2 = E2.data_ptr(), H2.data_ptr()
+        b.E2 = b.H2 = None
+        for f in range(6):
+            for c in range(2):
+                b.psi_e2[f][c] = None
+                b.psi_h2[f][c] = None
+        if mode is None or self._scratch is None:
+            return
+        E2, H2, pe2, ph2 = self._scratch
+        b.H2 = H2.data_ptr()
+        for f, (u, v) in enumerate(ph2):
+            b.psi_h2[f][0], b.psi_h2[f][1] = u.data_ptr(), v.data_ptr()
+        if mode == "fused":
+            b.E2 = E2.data_ptr()
             for f, (u, v) in enumerate(pe2):
                 b.psi_e2[f][0], b.psi_e2[f][1] = u.data_ptr(), v.data_ptr()
-            for f, (u, v) in enumerate(ph2):
-                b.psi_h2[f][0], b.psi_h2[f][1] = u.data_ptr(), v.data_ptr()
-        else:
-            b.E2 = b.H2 = None
-            for f in range(6):
-                for c in range(2):
-                    b.psi_e2[f][c] = None
-                    b.psi_h2[f][c] = None
 
-    def _ensure_scratch(self):
-        """Second copies of E, H and the CPML arrays, read and written alternately by the fused
-        multi-step kernel (allocated on the first fused run, kept for later ones)."""
-        if self._scratch is None:
-            E2 = torch.empty_like(self.E)
+    def _ensure_scratch(self, mode):
+        """Second copies of H and the H-side CPML arrays (the default run path) and, for the
+        fused path, of E and the E-side arrays; allocated on first use and kept."""
+        E2, H2, pe2, ph2 = self._scratch if self._scratch is not None else (None, None, None, None)
+        if H2 is None:
             H2 = torch.empty_like(self.H)
-            pe2 = [(torch.empty_like(u), torch.empty_like(v)) for u, v in self.psi["E"]]
             ph2 = [(torch.empty_like(u), torch.empty_like(v)) for u, v in self.psi["H"]]
-            self._scratch = (E2, H2, pe2, ph2)
+        if mode == "fused" and E2 is None:
+            E2 = torch.empty_like(self.E)
+            pe2 = [(torch.empty_like(u), torch.empty_like(v)) for u, v in self.psi["E"]]
+        self._scratch = (E2, H2, pe2, ph2)
 
     def _prepare(self, mat_key):
         _lib.check(self._lib.fdtd_prepare(self._plan, ctypes.byref(self._buf),
@@ -456,19 +462,22 @@ class Simulation:
     # ------------------------------------------------------------------------------------
     # additions beyond the reference
     # ------------------------------------------------------------------------------------
-    def run(self, nsteps: int, point_sources=None, wait_for=None, fused: bool = False,
-            monitor=None) -> Event:
+    def run(self, nsteps: int, point_sources=None, wait_for=None, monitor=None,
+            path: str = "auto") -> Event:
         """Advance ``nsteps`` canonical steps (E, F, point sources, H, G, S) in one call.
 
         ``point_sources`` is a list of (flat_index, values) pairs: after the E update of step
         t, ``E[flat_index] += values[t]`` (fdtd.py:168-169 without the host round trip).
         values are rounded to the field dtype, as the host-side ``+=`` does.
 
-        By default each step runs the per-update kernels (optionally over L2-resident x slabs,
-        see tune(slab=...)). With ``fused`` and no Bloch boundaries each step is instead one
-        fused kernel (E, sources, H and S in one pass, reading one copy of E, H and the CPML
-        arrays and writing a second); it moves about half the bytes but measured slower on
-        GB300. All give identical fields; the fused path refreshes oS on the last step only."""
+        ``path`` picks the kernels, all giving identical fields and S:
+          'auto'   'hs' where it applies (Poynting on, no Bloch boundaries), else 'plain';
+          'hs'     update_E in place, then H and S in one launch reading H (and the H-side
+                   CPML arrays) from one copy and writing a second: 96 B per cell per step;
+          'plain'  the per-update kernels (E, H, S), optionally over L2-resident x slabs
+                   (tune(slab=...));
+          'fused'  E, sources, H and S in one kernel per step (no Bloch boundaries).
+        The 'hs' and 'fused' paths write oS on the last step only."""
         nsteps = int(nsteps)
         stream = self._stream_handle(wait_for)
         src = None
@@ -491,11 +500,20 @@ class Simulation:
             idx_host = (ctypes.c_int64 * n)(*idx.tolist())
             keep = [val_t]
             src = _lib.FdtdPointSources(n, 0, ctypes.addressof(idx_host), val_t.data_ptr())
-        use_fused = fused and not self.bloch_boundaries
-        if use_fused:
-            self._ensure_scratch()
+        if path not in ("auto", "hs", "plain", "fused"):
+            raise ValueError("path must be 'auto', 'hs', 'plain' or 'fused'")
+        hs_ok = self.do_poynting and not self.bloch_boundaries
+        if path == "auto":
+            path = "hs" if hs_ok else "plain"
+        if path in ("hs", "fused") and self.bloch_boundaries:
+            raise ValueError("the '%s' path does not support Bloch boundaries" % path)
+        if path == "hs" and not self.do_poynting:
+            raise ValueError("the 'hs' path needs do_poynting=True")
+        mode = None if path == "plain" else path
+        if mode:
+            self._ensure_scratch(mode)
         bufs = self._buffers()
-        self._attach_scratch(use_fused)
+        self._attach_scratch(mode)
         mon = monitor.struct(nsteps) if monitor is not None else None
         _lib.check(self._lib.fdtd_run(self._plan, ctypes.byref(bufs),
                                       ctypes.c_void_p(stream.cuda_stream), nsteps,
@@ -557,11 +575,13 @@ class Simulation:
         return v.value or self.shape[0]
 
     def tune(self, xchunk: int = None, slab: int = None, fused_cells: int = None,
-             fused_xchunk: int = None):
+             fused_xchunk: int = None, hs_xchunk: int = None, hs_prefetch: bool = None):
         """Kernel tiling (None keeps a value); results do not depend on it."""
         for key, val in ((_lib.FDTD_TUNE_XCHUNK, xchunk), (_lib.FDTD_TUNE_SLAB, slab),
                          (_lib.FDTD_TUNE_FUSED_CELLS, fused_cells),
-                         (_lib.FDTD_TUNE_FUSED_XCHUNK, fused_xchunk)):
+                         (_lib.FDTD_TUNE_FUSED_XCHUNK, fused_xchunk),
+                         (_lib.FDTD_TUNE_HS_XCHUNK, hs_xchunk),
+                         (_lib.FDTD_TUNE_HS_PREFETCH, None if hs_prefetch is None else int(hs_prefetch))):
             if val is not None:
                 _lib.check(self._lib.fdtd_plan_tune(self._plan, key, int(val)))
 

@@ -63,6 +63,30 @@ def c2(float_type=numpy.float32, seed: int = 2, shape=None):
                         "8-cell CPML x6, Ey Gaussian pulse 1550 nm/20%%, Poynting on" % shape}
 
 
+def c3(float_type=numpy.float32, seed: int = 3, shape=(128, 128, 256)):
+    """Anisotropic + Bloch periodic cell: complex fields as split real/imaginary arrays, Bloch
+    phases kx = 0.3 pi / Lx and ky = 0.1 pi / Ly (phase k L across each period), 8-cell CPML
+    on the z faces only, diagonal eps in U[1, 12] and mu in U[1, 2] inside 12 seeded spheres
+    of radius 8-20 cells (one of them a perfect conductor), vacuum elsewhere, and a soft
+    plane-wave source (Ex on the whole z = 20 plane)."""
+    shape = tuple(shape)
+    eps, mu = geometry.sphere_inclusions(shape, n=12, rmin=8, rmax=20, seed=seed,
+                                         pec_index=5, dtype=float_type)
+    bloch = [{"axis": "x", "real": math.cos(0.3 * math.pi), "imag": math.sin(0.3 * math.pi)},
+             {"axis": "y", "real": math.cos(0.1 * math.pi), "imag": math.sin(0.1 * math.pi)}]
+    pmls = [{"axis": "z", "polarity": p, "thickness": 8} for p in "np"]
+    dt = 0.99 / math.sqrt(3)
+
+    def wave(t):
+        return math.sin(2 * math.pi * t * dt / 20.0) * math.exp(-0.5 * ((t - 80) / 25) ** 2)
+
+    return {"name": "c3", "shape": shape, "steps": 4000,
+            "kwargs": dict(epsilon=eps, mu=mu, pmls=pmls, bloch_boundaries=bloch,
+                           do_poynting=False, float_type=float_type),
+            "source_plane": 20, "wave": wave,
+            "describe": "%dx%dx%d complex (split f32), Bloch x/y, CPML z, eps/mu spheres, PEC sphere" % shape}
+
+
 def face_cells(shape, pmls) -> int:
     """Cells that carry a CPML auxiliary pair, summed over faces (corners count per face)."""
     total = 0
@@ -78,4 +102,4 @@ def face_cells(shape, pmls) -> int:
 
 
 def get(name: str, **kw):
-    return {"c1": c1, "c2": c2}[name](**kw)
+    return {"c1": c1, "c2": c2, "c3": c3}[name](**kw)

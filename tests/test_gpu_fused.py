@@ -54,8 +54,8 @@ def test_fused_equals_per_call_loop(name, tiles, nsteps):
     b = _gpu(**copy.deepcopy(kw))
     if tiles[0]:
         b.tune(fused_cells=tiles[0], fused_xchunk=tiles[1])
-    a.run(nsteps, point_sources=src, fused=False)
-    b.run(nsteps, point_sources=src, fused=True)
+    a.run(nsteps, point_sources=src, path="plain")
+    b.run(nsteps, point_sources=src, path="fused")
     _same_state(a, b, kw.get("do_poynting", True))
 
 
@@ -71,7 +71,7 @@ def test_fused_matches_oracle_with_mu_and_sources():
     kw = dict(epsilon=eps, mu=mu, pmls=pmls, do_poynting=True)
     g = _gpu(**copy.deepcopy(kw))
     g.tune(fused_cells=64, fused_xchunk=4)
-    g.run(steps, point_sources=srcs, fused=True)
+    g.run(steps, point_sources=srcs, path="fused")
     c = port.PortSimulation(nthreads=os.cpu_count(), **copy.deepcopy(kw))
     for t in range(steps):
         c.update_E()
@@ -90,8 +90,8 @@ def test_fused_then_per_call_continue_identically():
     src = _sources(kw, loop, 9)
     a = _gpu(**copy.deepcopy(kw))
     b = _gpu(**copy.deepcopy(kw))
-    a.run(9, point_sources=src, fused=False)
-    b.run(9, point_sources=src, fused=True)
+    a.run(9, point_sources=src, path="plain")
+    b.run(9, point_sources=src, path="fused")
     for s in (a, b):
         for _ in range(4):
             s.update_E([])
@@ -106,14 +106,14 @@ SLAB_CASES = [n for n in cases.CASE_NAMES if n != "fieldsrc"]
 @pytest.mark.parametrize("name", SLAB_CASES)
 @pytest.mark.parametrize("slab", [1, 2, 5, 0])
 def test_slab_schedule_equals_per_call_loop(name, slab):
-    """run(fused=False) advances the update kernels over x slabs (E, then H one plane
+    """run(path='plain') advances the update kernels over x slabs (E, then H one plane
     behind, then S); every slab width gives the per-call loop's state bit for bit."""
     kw, loop = cases.build(name)
     n = loop["steps"]
     a = cases.run_case(_gpu, name)
     b = _gpu(**copy.deepcopy(kw))
     b.tune(slab=slab)
-    b.run(n, point_sources=_sources(kw, loop, n), fused=False)
+    b.run(n, point_sources=_sources(kw, loop, n), path="plain")
     for k, v in cases.outputs(a, name).items():
         assert numpy.array_equal(v, _np(getattr(b, k))), k
     for fld in ("EHFG" if kw.get("bloch_boundaries") else "EH"):
@@ -136,6 +136,60 @@ def test_slab_schedule_bloch_mu():
     for slab in (1, 3, 0):
         b = _gpu(**copy.deepcopy(kw))
         b.tune(slab=slab)
-        b.run(12)
+        b.run(12, path="plain")
         for k in ("E", "H", "F", "G", "S"):
             assert torch.equal(getattr(a, k), getattr(b, k)), (slab, k)
+
+
+HS_SHAPES = [((16, 14, 12), 3), ((10, 9, 200), 3), ((6, 5, 511), 2), ((9, 11, 100), 4), ((7, 6, 300), 1)]
+
+
+@pytest.mark.parametrize("shape,T", HS_SHAPES)
+@pytest.mark.parametrize("xchunk", [1, 3, 8])
+@pytest.mark.parametrize("nsteps", [5, 8])
+def test_hs_path_equals_per_call_loop(shape, T, xchunk, nsteps):
+    """run(path='hs'): H and S in one launch, with blocks of whole z rows so that several
+    blocks (and, for sz > 256, one-row blocks) recompute their first row's y-1 products."""
+    rng = numpy.random.default_rng(sum(shape) + T)
+    eps = [rng.uniform(1, 4, shape).astype(numpy.float32) for _ in range(3)]
+    eps[1][1:3, 2:4, 5:9] = numpy.inf
+    init = {k: [rng.standard_normal(shape).astype(numpy.float32) for _ in range(3)] for k in "EH"}
+    pmls = [{"axis": a, "polarity": p, "thickness": T} for a in "xyz" for p in "np"
+            if 2 * T <= shape["xyz".index(a)]]
+    kw = dict(epsilon=eps, pmls=pmls, initial_fields=init, do_poynting=True)
+    N = int(numpy.prod(shape))
+    src = [(int(rng.integers(0, 3 * N)), [math.sin(0.3 * t) for t in range(nsteps)])]
+    a = _gpu(**copy.deepcopy(kw))
+    b = _gpu(**copy.deepcopy(kw))
+    b.tune(hs_xchunk=xchunk, hs_prefetch=bool(xchunk % 2))
+    a.run(nsteps, point_sources=src, path="plain")
+    b.run(nsteps, point_sources=src, path="hs")
+    _same_state(a, b, True)
+
+
+@pytest.mark.parametrize("name", ["c1_small", "pml_mixed", "periodic_pec_poynting", "nonuniform", "dx_half", "f64_mixed"])
+def test_hs_path_cases(name):
+    kw, loop = cases.build(name)
+    if not kw.get("do_poynting", True):
+        kw["do_poynting"] = True
+    n = loop["steps"]
+    src = _sources(kw, loop, n)
+    a = _gpu(**copy.deepcopy(kw))
+    b = _gpu(**copy.deepcopy(kw))
+    a.run(n, point_sources=src, path="plain")
+    b.run(n, point_sources=src, path="hs")
+    _same_state(a, b, True)
+
+
+def test_hs_path_with_mu():
+    shape = (18, 16, 20)
+    eps, mu = geometry.sphere_inclusions(shape, n=4, rmin=2, rmax=5, seed=31, pec_index=2)
+    pmls = [{"axis": a, "polarity": p, "thickness": 3} for a in "xyz" for p in "np"]
+    kw = dict(epsilon=eps, mu=mu, pmls=pmls, do_poynting=True)
+    N = int(numpy.prod(shape))
+    src = [(int(numpy.ravel_multi_index((9, 8, 10), shape)) + 2 * N, [math.sin(0.4 * t) for t in range(21)])]
+    a = _gpu(**copy.deepcopy(kw))
+    b = _gpu(**copy.deepcopy(kw))
+    a.run(21, point_sources=src, path="plain")
+    b.run(21, point_sources=src, path="hs")
+    _same_state(a, b, True)
