@@ -148,7 +148,10 @@ def algorithmic_bytes(N: int, face_cells: int, elem: int, poynting: bool):
         h += N * 6 * elem                                 # oS w
         s = N * 9 * elem                                  # oS r, S w
     step = N * 21 * elem + face_cells * 8 * elem + (N * 3 * elem if poynting else 0)
-    return {"k_bulk_e": e, "k_bulk_h": h, "k_bulk_s": s}, step
+    # run()'s H+S kernel: H read (one copy) and written (the other), E read, S written;
+    # psi_H read / written
+    hs = N * 12 * elem + face_cells * 4 * elem
+    return {"k_bulk_e": e, "k_bulk_h": h, "k_bulk_s": s, "k_bulk_hs": hs}, step
 
 
 def cpu_sample(wl, seconds: float, nthreads: int):
@@ -301,6 +304,30 @@ def time_run(sim, lib, wave_dev, ind, K, W, world, mode):
     return e0.elapsed_time(e1)
 
 
+def run_kernel_ms(sim, lib, wave_dev, ind, steps):
+    """Mean launch times of the H+S path's two kernels: one more fdtd_run with the plan's
+    timing events on (CUDA events on the launching stream around update_E and the H+S kernel
+    of up to 64 sampled steps)."""
+    import torch
+    from opencl_fdtd_gb300 import _lib
+    stream = sim.queue
+    sim._ensure_scratch("hs")
+    bufs = sim._buffers()
+    sim._attach_scratch("hs")
+    idx = (ctypes.c_int64 * 1)(ind)
+    src = _lib.FdtdPointSources(1, 0, ctypes.addressof(idx), wave_dev.data_ptr())
+    _lib.check(lib.fdtd_plan_tune(sim._plan, _lib.FDTD_TUNE_TIMING, 1))
+    with torch.cuda.stream(stream):
+        _lib.check(lib.fdtd_run(sim._plan, ctypes.byref(bufs), ctypes.c_void_p(stream.cuda_stream),
+                                steps, ctypes.byref(src), None))
+    torch.cuda.synchronize()
+    _lib.check(lib.fdtd_plan_tune(sim._plan, _lib.FDTD_TUNE_TIMING, 0))
+    ms = (ctypes.c_double * 2)()
+    n = ctypes.c_int32()
+    _lib.check(lib.fdtd_run_kernel_ms(sim._plan, ms, ctypes.byref(n)))
+    return {"k_bulk_e": ms[0], "k_bulk_hs": ms[1]}, n.value
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -347,6 +374,7 @@ def main():
         res["dropin"] = time_dropin(sim, lib, wave_dev, ind, K, W, poynting, world)
     if args.path in ("hs", "default", "all") and poynting:
         res["hs"] = time_run(sim, lib, wave_dev, ind, K, W, world, "hs")
+        hs_per = run_kernel_ms(sim, lib, wave_dev, ind, min(W + K, 640))
     if args.path in ("slab", "all"):
         res["slab"] = time_run(sim, lib, wave_dev, ind, K, W, world, None)
         sim.tune(slab=0)
@@ -399,6 +427,17 @@ def main():
                          "compulsory_bytes_per_step": compulsory,
                          "compulsory_frac": round(compulsory / (ms * 1e-3) / 1e9 / peak, 4),
                          "mean_step_ms": round(ms, 5)}}
+    if "hs" in out_paths:
+        per, nsamp = hs_per
+        dom = max(per, key=lambda k: per[k])
+        ach = per_launch[dom] / (per[dom] * 1e-3) / 1e9
+        out_paths["hs"]["kernel_roofline"] = {
+            "bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(ach / peak, 4), "peak_source": peak_kind, "traffic": traffic.get(dom),
+            "algorithmic_bytes_per_launch": per_launch[dom], "mean_launch_ms": round(per[dom], 5),
+            "per_kernel_ms": {k: round(v, 5) for k, v in per.items()}, "sampled_launches": nsamp,
+            "per_kernel_frac": {k: round(per_launch[k] / (v * 1e-3) / 1e9 / peak, 4)
+                                for k, v in per.items()}}
     cands = [n for n in ("fused", "slab", "hs") if n in out_paths]
     head = min(cands, key=lambda n: out_paths[n]["ms_per_step"]) if cands else "dropin"
     hp = out_paths[head]
@@ -430,12 +469,15 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             # the dominant kernel's roofline: per-call timing of the same kernels the run
             # path launches (the fused path reports its own kernel)
-            "roofline": (out_paths["dropin"]["roofline"] if head != "fused" and "dropin" in out_paths
+            # the dominant kernel of the headline path, timed per launch with CUDA events
+            "roofline": (hp["kernel_roofline"] if "kernel_roofline" in hp else
+                         out_paths["dropin"]["roofline"] if head != "fused" and "dropin" in out_paths
                          else hp["roofline"]),
             "step_roofline": {"achieved": round(step_gbs, 1), "peak": peak, "unit": "GB/s",
                               "frac": round(step_gbs / peak, 4), "bytes_per_step": step_bytes},
             "clocks": clock, "e2e": e2e, "gpu_launches": hp["gpu_launches"],
             "cpu_baseline": cpu,
+            "dropin_roofline": out_paths["dropin"]["roofline"] if "dropin" in out_paths else None,
             "paths": {k: {"value": round(v["value"], 2), "ms_per_step": round(v["ms_per_step"], 5),
                           "roofline_frac": v["roofline"]["frac"], "kernel": v["roofline"]["kernel"]}
                       for k, v in out_paths.items()},

@@ -125,13 +125,17 @@ int fdtd_plan_destroy(FdtdPlan *plan);
  *   FUSED_XCHUNK  x planes one block of the fused step marches (default 16)
  *   HS_XCHUNK     x planes one block of the H+S kernel of fdtd_run marches (default 16)
  *   HS_PREFETCH   1: the H+S kernel loads the next plane ahead (one block per SM); 0: not
- *                 (two blocks per SM, the default) */
+ *                 (two blocks per SM, the default)
+ *   TIMING        1: fdtd_run's H+S path records CUDA events around its update_E and H+S
+ *                 kernels on up to 64 steps spread over the call and waits for the stream
+ *                 before it returns (profiling; read with fdtd_run_kernel_ms); 0 (default) */
 #define FDTD_TUNE_XCHUNK 1
 #define FDTD_TUNE_SLAB 2
 #define FDTD_TUNE_FUSED_CELLS 3
 #define FDTD_TUNE_FUSED_XCHUNK 4
 #define FDTD_TUNE_HS_XCHUNK 5
 #define FDTD_TUNE_HS_PREFETCH 6
+#define FDTD_TUNE_TIMING 7
 int fdtd_plan_tune(FdtdPlan *plan, int32_t key, int32_t value);
 /* Current value of a tuning key. */
 int fdtd_plan_get(const FdtdPlan *plan, int32_t key, int32_t *value);
@@ -221,6 +225,11 @@ int fdtd_energy(FdtdPlan *plan, const FdtdBuffers *buf, double *scratch, int32_t
  * oS is then written on the last step only. */
 int fdtd_run(FdtdPlan *plan, const FdtdBuffers *buf, void *stream, int32_t nsteps,
              const FdtdPointSources *src, FdtdDftMonitor *mon);
+
+/* Mean launch time in ms of update_E (ms[0]) and of the H+S kernel (ms[1]) over the sampled
+ * steps of the last fdtd_run made on the H+S path with FDTD_TUNE_TIMING on, and the number of
+ * samples (0 if none). Profiling aid; no counterpart in the reference. */
+int fdtd_run_kernel_ms(const FdtdPlan *plan, double ms[2], int32_t *samples);
 
 #ifdef __cplusplus
 }

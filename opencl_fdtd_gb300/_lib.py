@@ -29,6 +29,7 @@ FDTD_TUNE_FUSED_CELLS = 3
 FDTD_TUNE_FUSED_XCHUNK = 4
 FDTD_TUNE_HS_XCHUNK = 5
 FDTD_TUNE_HS_PREFETCH = 6
+FDTD_TUNE_TIMING = 7
 
 
 class FdtdPmlDesc(ctypes.Structure):
@@ -93,6 +94,7 @@ SIGNATURES = [
     ("fdtd_plane_sum_noalloc", c_i32, [c_vp, c_vp, c_i32, c_i32, c_i64, c_i32, c_vp, c_vp]),
     ("fdtd_run", c_i32, [c_vp, _P(FdtdBuffers), c_vp, c_i32, _P(FdtdPointSources),
                          _P(FdtdDftMonitor)]),
+    ("fdtd_run_kernel_ms", c_i32, [c_vp, _P(c_f64), _P(c_i32)]),
 ]
 
 _LIB = None

@@ -279,6 +279,69 @@ int run_point_sources(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st,
     return check_cuda(launch_point_sources<R>(k, st), "point source launch");
 }
 
+// Profiling aid of fdtd_run (FDTD_TUNE_TIMING): CUDA events on the launching stream around the
+// two kernels of up to 64 steps spread over the call; finish() waits for the stream and stores
+// the mean launch times in the plan. Inactive (no events, no waiting) when timing is off.
+class KernelTimer {
+  public:
+    static constexpr int MAX_SAMPLES = 64;
+    KernelTimer(FdtdPlan *p, int nsteps, cudaStream_t st) : p_(p), st_(st), n_(0), stride_(0)
+    {
+        if (p->timing && nsteps > 0) stride_ = (nsteps + MAX_SAMPLES - 1) / MAX_SAMPLES;
+        nsteps_ = nsteps;
+    }
+    ~KernelTimer()
+    {
+        for (int s = 0; s < n_; ++s)
+            for (int c = 0; c < 4; ++c) cudaEventDestroy(ev_[s][c]);
+    }
+    int init()
+    {
+        if (!stride_) return FDTD_OK;
+        for (int s = 0; s < MAX_SAMPLES && s * stride_ < nsteps_; ++s) {
+            for (int c = 0; c < 4; ++c) {
+                const cudaError_t e = cudaEventCreate(&ev_[s][c]);
+                if (e != cudaSuccess) {
+                    for (int q = 0; q < c; ++q) cudaEventDestroy(ev_[s][q]);
+                    return check_cuda(e, "timing event");
+                }
+            }
+            ++n_;
+        }
+        return FDTD_OK;
+    }
+    // c: 0/1 around update_E, 2/3 around the H+S kernel
+    int mark(int t, int c)
+    {
+        if (!stride_ || t % stride_) return FDTD_OK;
+        return check_cuda(cudaEventRecord(ev_[t / stride_][c], st_), "timing event");
+    }
+    int finish()
+    {
+        if (!n_) return FDTD_OK;
+        int rc = check_cuda(cudaStreamSynchronize(st_), "timing sync");
+        if (rc) return rc;
+        double se = 0.0, sh = 0.0;
+        for (int s = 0; s < n_; ++s) {
+            float me = 0.f, mh = 0.f;
+            if ((rc = check_cuda(cudaEventElapsedTime(&me, ev_[s][0], ev_[s][1]), "timing read"))) return rc;
+            if ((rc = check_cuda(cudaEventElapsedTime(&mh, ev_[s][2], ev_[s][3]), "timing read"))) return rc;
+            se += me;
+            sh += mh;
+        }
+        p_->kernel_ms[0] = se / n_;
+        p_->kernel_ms[1] = sh / n_;
+        p_->kernel_samples = n_;
+        return FDTD_OK;
+    }
+
+  private:
+    FdtdPlan *p_;
+    cudaStream_t st_;
+    int n_, stride_, nsteps_;
+    cudaEvent_t ev_[MAX_SAMPLES][4];
+};
+
 // Multi-step path with the H+S kernel: update_E in place, point sources, then H and S in one
 // launch that reads H (and the H-side psi) from one copy and writes the other; the copies
 // swap every step and the state is brought home after an odd number of steps.
@@ -318,10 +381,14 @@ int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
     FdtdBuffers bb = *b;
     void *H[2] = {b->H, b->H2};
     int rc;
+    KernelTimer timer(p, nsteps, st);
+    if ((rc = timer.init())) return rc;
     for (int t = 0; t < nsteps; ++t) {
         const int a = t & 1, o = a ^ 1;
         bb.H = H[a];
+        if ((rc = timer.mark(t, 0))) return rc;
         if ((rc = run_update_e<R>(p, &bb, st, false))) return rc;
+        if ((rc = timer.mark(t, 1))) return rc;
         if (src && src->n > 0 && (rc = run_point_sources<R>(p, &bb, st, src, t))) return rc;
         k.E = (const R *)b->E;
         k.HA = (const R *)H[a];
@@ -338,9 +405,12 @@ int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
                 }
             }
         k.write_oS = t == nsteps - 1;
+        if ((rc = timer.mark(t, 2))) return rc;
         if ((rc = check_cuda(launch_hs<R>(k, p->d.has_mu != 0, dxmode, p->hs_prefetch != 0, st), "H+S launch"))) return rc;
+        if ((rc = timer.mark(t, 3))) return rc;
         if (mon && (rc = run_dft<R>(p, b->E, st, mon, t))) return rc;
     }
+    if ((rc = timer.finish())) return rc;
     if (nsteps & 1) {
         const size_t fb = 3 * (size_t)p->N * p->elem;
         rc = check_cuda(cudaMemcpyAsync(b->H, b->H2, fb, cudaMemcpyDeviceToDevice, st), "copy H");
@@ -652,6 +722,9 @@ int fdtd_plan_create(const FdtdDesc *desc, FdtdPlan **out)
     p->fused_cells = 0;
     p->hs_xchunk = 16;
     p->hs_prefetch = 0;
+    p->timing = 0;
+    p->kernel_ms[0] = p->kernel_ms[1] = 0.0;
+    p->kernel_samples = 0;
     p->fused_xchunk = 16;
     cudaGetDevice(&p->device);
     size_t total = 0;
@@ -720,6 +793,10 @@ int fdtd_plan_tune(FdtdPlan *p, int32_t key, int32_t value)
         if (value < 1 || value > 4096) return fail(FDTD_ERR_INVALID, "hs_xchunk must be in [1, 4096]");
         p->hs_xchunk = (uint32_t)value;
         return FDTD_OK;
+    case FDTD_TUNE_TIMING:
+        if (value != 0 && value != 1) return fail(FDTD_ERR_INVALID, "timing must be 0 or 1");
+        p->timing = value;
+        return FDTD_OK;
     case FDTD_TUNE_HS_PREFETCH:
         if (value != 0 && value != 1) return fail(FDTD_ERR_INVALID, "hs_prefetch must be 0 or 1");
         p->hs_prefetch = value;
@@ -739,6 +816,7 @@ int fdtd_plan_get(const FdtdPlan *p, int32_t key, int32_t *value)
     case FDTD_TUNE_FUSED_XCHUNK: *value = (int32_t)p->fused_xchunk; return FDTD_OK;
     case FDTD_TUNE_HS_XCHUNK: *value = (int32_t)p->hs_xchunk; return FDTD_OK;
     case FDTD_TUNE_HS_PREFETCH: *value = p->hs_prefetch; return FDTD_OK;
+    case FDTD_TUNE_TIMING: *value = p->timing; return FDTD_OK;
     default: return fail(FDTD_ERR_INVALID, "unknown tuning key");
     }
 }
@@ -978,6 +1056,15 @@ int fdtd_run(FdtdPlan *p, const FdtdBuffers *b, void *stream, int32_t nsteps,
     rc = f64 ? run_slabs<double>(p, b, st, nsteps, src, mon) : run_slabs<float>(p, b, st, nsteps, src, mon);
     if (!rc && mon) { mon->step += nsteps; mon->series_row += nsteps; }
     return rc;
+}
+
+int fdtd_run_kernel_ms(const FdtdPlan *p, double ms[2], int32_t *samples)
+{
+    if (!p || !ms || !samples) return fail(FDTD_ERR_INVALID, "fdtd_run_kernel_ms: NULL pointer");
+    ms[0] = p->kernel_ms[0];
+    ms[1] = p->kernel_ms[1];
+    *samples = p->kernel_samples;
+    return FDTD_OK;
 }
 
 }  // extern "C"

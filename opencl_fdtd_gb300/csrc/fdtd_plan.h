@@ -18,6 +18,9 @@ struct FdtdPlan {
     uint32_t fused_xchunk;      // x planes one block of the fused step marches
     uint32_t hs_xchunk;         // x planes one block of the H+S kernel marches
     int32_t hs_prefetch;        // H+S kernel issues the next plane's loads early
+    int32_t timing;             // fdtd_run's H+S path records per-kernel CUDA events
+    double kernel_ms[2];        // last timed run: mean update_E and H+S launch times (ms)
+    int32_t kernel_samples;     // launches each mean is over
     void *coef = nullptr;       // device copy of every face's six coefficient tables
     const void *tab[6][6];      // per face: p0e p1e p2e p0h p1h p2h (device pointers)
 };
