@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--slab", type=int, default=-1, help="x planes per L2 slab (-1: plan default)")
     ap.add_argument("--hs-xchunk", type=int, default=0)
     ap.add_argument("--hs-prefetch", type=int, default=-1)
+    ap.add_argument("--c4-variants", type=int, default=64, help="c4: number of cavity variants")
+    ap.add_argument("--c4-steps", type=int, default=2000, help="c4: steps of every variant")
+    ap.add_argument("--c4-chunk", type=int, default=100, help="c4: steps per captured launch")
     ap.add_argument("--path", choices=["fused", "slab", "hs", "dropin", "default", "all"], default="default",
                     help="default = per-call loop (per-kernel timing) + Simulation.run (hs path); "
                          "slab = run over the per-update kernels; fused = the opt-in fused step")
@@ -547,5 +550,152 @@ def run_e2e(sim, wl, steps: int, world: int, run_api: bool = False, path: str = 
             "api": "Simulation.update_E/H/S + tensor source add, stream-ordered"}
 
 
+def _peak_frequency(series, dt, w0):
+    """Angular frequency of the largest spectral peak within [0.5 w0, 1.5 w0] of a sampled
+    series (zero-padded FFT, parabolic interpolation of the log magnitude)."""
+    x = numpy.asarray(series, dtype=numpy.float64)
+    n = 1 << 18
+    spec = numpy.abs(numpy.fft.rfft(x, n))
+    w = 2 * numpy.pi * numpy.fft.rfftfreq(n, dt)
+    band = numpy.flatnonzero((w > 0.5 * w0) & (w < 1.5 * w0))
+    k = band[numpy.argmax(spec[band])]
+    if 0 < k < len(spec) - 1 and spec[k - 1] > 0 and spec[k + 1] > 0:
+        a, b, c = numpy.log(spec[k - 1]), numpy.log(spec[k]), numpy.log(spec[k + 1])
+        den = a - 2 * b + c
+        off = 0.5 * (a - c) / den if den != 0 else 0.0
+        return float(w[k] + off * (w[1] - w[0]))
+    return float(w[k])
+
+
+def run_c4(args):
+    """Batched sweep: per-variant Simulation.run against one persistent launch per chunk of
+    steps (CUDA graph replays, autotuned tiles) in float32, bfloat16 and float16 storage; the
+    16-bit errors against a float64 run of every variant (relative L2 of E, DFT-peak
+    frequency of the centre E_y series)."""
+    import torch
+    from opencl_fdtd_gb300 import Simulation, workloads
+    from opencl_fdtd_gb300.batch import BatchSimulation
+    torch.cuda.set_device(0)
+    steps, chunk = args.c4_steps, args.c4_chunk
+    if steps % chunk:
+        raise SystemExit("--c4-steps must be a multiple of --c4-chunk")
+    t_setup = time.perf_counter()
+    variants = workloads.c4(n=args.c4_variants, steps=steps)
+    kws, idx = [], []
+    for var in variants:
+        kw, ind = workloads.c4_kwargs(var)
+        kws.append(kw)
+        idx.append(ind)
+    sims = [Simulation(**kw) for kw in kws]
+    wave = numpy.array([variants[0]["wave"](t) for t in range(steps)], dtype=numpy.float64)
+    cells = sum(s.N for s in sims)
+    interior = sum(max(s.shape[0] - 16, 0) * max(s.shape[1] - 16, 0) * max(s.shape[2] - 16, 0) for s in sims)
+    sources = [[(ind, wave)] for ind in idx]
+    monitors = [[ind] for ind in idx]
+    setup_s = time.perf_counter() - t_setup
+    stream = sims[0].queue
+
+    def reset():
+        for s in sims:
+            s.E.zero_()
+            s.H.zero_()
+            for f in ("E", "H"):
+                for u, v in s.psi[f]:
+                    u.zero_()
+                    v.zero_()
+            s.steps_run = 0
+        torch.cuda.synchronize()
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    out = {"plain": {}, "batched": {}}
+    # per-variant Simulation.run, one after the other on one stream
+    mons = [s.dft_monitor([(1, tuple(c // 2 for c in s.shape))], ()) for s in sims]
+
+    def plain():
+        for s, src, m in zip(sims, sources, mons):
+            s.run(steps, point_sources=src, monitor=m, path="plain")
+    ms = timed(plain)
+    out["plain"] = {"ms": round(ms, 3), "value": round(cells * steps / (ms * 1e-3) / 1e6, 2),
+                    "interior_value": round(interior * steps / (ms * 1e-3) / 1e6, 2),
+                    "launches": len(sims) * steps * 3}
+    plain_E = [s.E.clone() for s in sims]
+    plain_series = [m.series()[:, 0] for m in mons]
+    results = {}
+    for storage in ("f32", "bf16", "fp16"):
+        reset()
+        b = BatchSimulation(sims, storage=storage, sources=sources, monitors=monitors, steps=steps)
+        tune = b.autotune(steps=10)
+        b.capture(chunk)
+        ms = timed(lambda: [b.replay() for _ in range(steps // chunk)])
+        b.sync()
+        torch.cuda.synchronize()
+        results[storage] = {"E": [s.E.clone() for s in sims], "series": [x.cpu().numpy()[:, 0] for x in b.series]}
+        out["batched"][storage] = {
+            "ms": round(ms, 3), "value": round(cells * steps / (ms * 1e-3) / 1e6, 2),
+            "interior_value": round(interior * steps / (ms * 1e-3) / 1e6, 2),
+            "tiles": {"schedule": tune["schedule"], "xchunk": tune["xchunk"],
+                      "blocks_per_sm": tune["blocks_per_sm"], "autotune_ms_per_step": tune.get("timings")},
+            "launches": steps // chunk if tune["schedule"] == "persistent" else 2 * steps,
+            "steps_per_graph": chunk, "graph_replays": steps // chunk}
+        b.close()
+        del b
+    out["batched"]["f32"]["bit_identical_to_plain"] = all(
+        torch.equal(a, c) for a, c in zip(plain_E, results["f32"]["E"])) and all(
+        numpy.array_equal(a, c) for a, c in zip(plain_series, results["f32"]["series"]))
+    # float64 reference of every variant: errors of the float32 and 16-bit runs
+    w0 = 2 * math.pi * 40.0 / 1550.0
+    err = {k: {"rel_l2": [], "peak_rel": []} for k in ("f32", "bf16", "fp16")}
+    for v, var in enumerate(variants):
+        kw64, ind = workloads.c4_kwargs(var, float_type=numpy.float64)
+        s64 = Simulation(**kw64)
+        m64 = s64.dft_monitor([(1, tuple(c // 2 for c in s64.shape))], ())
+        s64.run(steps, point_sources=[(ind, wave)], monitor=m64, path="plain")
+        ref = s64.E
+        fin = torch.isfinite(ref)
+        nref = torch.linalg.norm(ref[fin])
+        w_ref = _peak_frequency(m64.series()[:, 0], s64.dt, w0)
+        for k in err:
+            e = results[k]["E"][v].double()
+            err[k]["rel_l2"].append(float(torch.linalg.norm((e - ref)[fin]) / nref))
+            err[k]["peak_rel"].append(abs(_peak_frequency(results[k]["series"][v], s64.dt, w0) - w_ref) / w_ref)
+        del s64, m64, ref
+    for k in err:
+        a = numpy.array(err[k]["rel_l2"])
+        p = numpy.array(err[k]["peak_rel"])
+        out["batched"][k]["error_vs_f64"] = {
+            "rel_l2_E": {"median": float(numpy.median(a)), "max": float(a.max())},
+            "dft_peak_rel": {"median": float(numpy.median(p)), "max": float(p.max())},
+            "per_variant_rel_l2_E": [float("%.3g" % x) for x in a],
+            "per_variant_dft_peak_rel": [float("%.3g" % x) for x in p]}
+    best = out["batched"]["f32"]
+    line = {
+        "metric": METRIC, "value": best["value"], "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": 10,
+        "ms_per_step": round(best["ms"] / steps, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 arithmetic; f32 / bf16 / fp16 storage", "data": "synthetic (seeded L3 variants)",
+        "config": {"workload": "c4: %d seeded L3-cavity variants, grids U{96..256}xU{96..224}xU{48..73}, "
+                               "a ~ U[8,12], r ~ U[0.25a,0.35a], 8-cell CPML x6, Poynting off, %d steps"
+                               % (len(variants), steps),
+                   "cells": cells, "interior_cells": interior, "setup_s": round(setup_s, 1),
+                   "l2": "inputs (%.1f GB of fields) larger than the 129 MB L2; no flush" % (cells * 36 / 1e9)},
+        "plain": out["plain"], "batched": out["batched"],
+        "speedup_batched_f32_vs_plain": round(out["plain"]["ms"] / best["ms"], 3),
+    }
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
-    main()
+    _a = parse()
+    if _a.workload == "c4" and _a.impl == "ours":
+        run_c4(_a)
+    else:
+        main()

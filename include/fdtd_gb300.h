@@ -231,6 +231,69 @@ int fdtd_run(FdtdPlan *plan, const FdtdBuffers *buf, void *stream, int32_t nstep
  * samples (0 if none). Profiling aid; no counterpart in the reference. */
 int fdtd_run_kernel_ms(const FdtdPlan *plan, double ms[2], int32_t *samples);
 
+/* ---- batched stepping of many independent variants (one persistent launch) ---------------
+ * No counterpart in the reference, which steps one grid per Simulation. Each variant is a
+ * grid with diagonal eps (no mu, no Bloch boundaries, no Poynting, uniform dx) whose E, H and
+ * dt/eps arrays are stored in float32, bfloat16 or float16 (arithmetic is float32 in every
+ * case); the CPML psi arrays are float32. With float32 storage the results are bit-identical
+ * to stepping each variant on its own with fdtd_run. In 16-bit storage every run of 32
+ * consecutive (y, z) cells of one component in one x plane carries a power-of-two exponent e
+ * (stored = value * 2^-e), chosen when the run is written. e_exp / h_exp are int32
+ * [sx][ceil(sy*sz/32)]: one word per run holds the three components' exponents as the bytes
+ * e_c + 128 at bits 8c .. 8c + 7. */
+#define FDTD_STORE_F32 0
+#define FDTD_STORE_BF16 1
+#define FDTD_STORE_F16 2
+#define FDTD_BATCH_MAX_SRC 4
+#define FDTD_BATCH_MAX_MON 8
+
+typedef struct FdtdBatchFace {
+    int32_t axis, polarity, thickness, _pad;
+    const float *tab_e[3], *tab_h[3];  /* device p0 p1 p2 of the E and H updates, T each */
+    float *psi_e[2], *psi_h[2];        /* device psi (u, v) of the face, layout of FdtdBuffers */
+} FdtdBatchFace;
+
+typedef struct FdtdBatchVariant {
+    int32_t shape[3], n_pml;
+    double dt, dx;
+    FdtdBatchFace pml[6];
+    void *E, *H;                       /* device 3N each, storage type */
+    const void *ce;                    /* device 3N dt/eps, storage type */
+    int32_t *e_exp, *h_exp;            /* device tile exponents (16-bit storage), else NULL */
+    int32_t n_src, n_mon;
+    int64_t src_index[FDTD_BATCH_MAX_SRC];   /* flat indices into E (c*N + cell) */
+    const float *src_values;           /* device [rows][n_src]: row = step number */
+    int64_t mon_index[FDTD_BATCH_MAX_MON];   /* flat indices into E */
+    double *series;                    /* device [rows][n_mon] or NULL: E after each step */
+} FdtdBatchVariant;
+
+typedef struct FdtdBatch FdtdBatch;
+
+/* Validate n variants and build the tile list (x chunks of xchunk planes, default 8). rows:
+ * rows of every variant's src_values / series (steps past it add no source, record nothing). */
+int fdtd_batch_create(const FdtdBatchVariant *vars, int32_t n, int32_t storage, int64_t rows,
+                      FdtdBatch **out);
+int fdtd_batch_destroy(FdtdBatch *batch);
+/* Tile shape and grid: x planes per tile (>= 1) and resident blocks per SM (0: the most that
+ * fit). Rebuilds the tile list. */
+int fdtd_batch_tune(FdtdBatch *batch, int32_t xchunk, int32_t blocks_per_sm);
+/* Advance every variant by nsteps steps (E, sources, H per step) on the stream: with the
+ * FDTD_BATCH_LAUNCHES schedule (default) as two launches per step, each covering the tiles of
+ * every variant; with FDTD_BATCH_PERSISTENT as one cooperative launch for all nsteps steps.
+ * The step counter lives on the device (read and advanced by the launches), so captured
+ * launches keep counting when a CUDA graph replays them. */
+#define FDTD_BATCH_PERSISTENT 0
+#define FDTD_BATCH_LAUNCHES 1
+int fdtd_batch_schedule(FdtdBatch *batch, int32_t schedule);
+int fdtd_batch_run(FdtdBatch *batch, void *stream, int32_t nsteps);
+/* Read / set the batch's device step counter (waits for the device). */
+int fdtd_batch_get_step(FdtdBatch *batch, int64_t *step);
+int fdtd_batch_set_step(FdtdBatch *batch, int64_t step);
+/* 16-bit storage: float32 field (0 = E, 1 = H) of variant v -> storage with fresh tile
+ * exponents, and back. */
+int fdtd_batch_encode(FdtdBatch *batch, int32_t v, int32_t field, const float *src, void *stream);
+int fdtd_batch_decode(FdtdBatch *batch, int32_t v, int32_t field, float *dst, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

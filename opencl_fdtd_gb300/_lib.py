@@ -72,6 +72,24 @@ class FdtdDftMonitor(ctypes.Structure):
                 ("accum", c_vp), ("series", c_vp), ("step", c_i64), ("series_row", c_i64)]
 
 
+FDTD_STORE_F32, FDTD_STORE_BF16, FDTD_STORE_F16 = 0, 1, 2
+FDTD_BATCH_MAX_SRC, FDTD_BATCH_MAX_MON = 4, 8
+FDTD_BATCH_PERSISTENT, FDTD_BATCH_LAUNCHES = 0, 1
+
+
+class FdtdBatchFace(ctypes.Structure):
+    _fields_ = [("axis", c_i32), ("polarity", c_i32), ("thickness", c_i32), ("_pad", c_i32),
+                ("tab_e", c_vp * 3), ("tab_h", c_vp * 3), ("psi_e", c_vp * 2), ("psi_h", c_vp * 2)]
+
+
+class FdtdBatchVariant(ctypes.Structure):
+    _fields_ = [("shape", c_i32 * 3), ("n_pml", c_i32), ("dt", c_f64), ("dx", c_f64),
+                ("pml", FdtdBatchFace * 6), ("E", c_vp), ("H", c_vp), ("ce", c_vp),
+                ("e_exp", c_vp), ("h_exp", c_vp), ("n_src", c_i32), ("n_mon", c_i32),
+                ("src_index", c_i64 * FDTD_BATCH_MAX_SRC), ("src_values", c_vp),
+                ("mon_index", c_i64 * FDTD_BATCH_MAX_MON), ("series", c_vp)]
+
+
 # (name, restype, argtypes) of every entry point in include/fdtd_gb300.h
 _P = ctypes.POINTER
 SIGNATURES = [
@@ -95,6 +113,15 @@ SIGNATURES = [
     ("fdtd_run", c_i32, [c_vp, _P(FdtdBuffers), c_vp, c_i32, _P(FdtdPointSources),
                          _P(FdtdDftMonitor)]),
     ("fdtd_run_kernel_ms", c_i32, [c_vp, _P(c_f64), _P(c_i32)]),
+    ("fdtd_batch_create", c_i32, [_P(FdtdBatchVariant), c_i32, c_i32, c_i64, _P(c_vp)]),
+    ("fdtd_batch_destroy", c_i32, [c_vp]),
+    ("fdtd_batch_tune", c_i32, [c_vp, c_i32, c_i32]),
+    ("fdtd_batch_schedule", c_i32, [c_vp, c_i32]),
+    ("fdtd_batch_run", c_i32, [c_vp, c_vp, c_i32]),
+    ("fdtd_batch_get_step", c_i32, [c_vp, _P(c_i64)]),
+    ("fdtd_batch_set_step", c_i32, [c_vp, c_i64]),
+    ("fdtd_batch_encode", c_i32, [c_vp, c_i32, c_i32, c_vp, c_vp]),
+    ("fdtd_batch_decode", c_i32, [c_vp, c_i32, c_i32, c_vp, c_vp]),
 ]
 
 _LIB = None

@@ -32,6 +32,8 @@ UNITS = {
     "yee_kernels.cu": ["--fmad=false"],
     "step_fused.cu": ["--fmad=false"],
     "hs_fused.cu": ["--fmad=false"],
+    "batch.cu": ["--fmad=false"],
+    "batch_abi.cu": [],
     "monitors.cu": [],
     "noalloc.cu": [],
     "fdtd_abi.cu": [],

@@ -193,6 +193,7 @@ class Simulation:
             self.Jr = torch.zeros_like(self.E)
 
         self._create_pmls(pmls)
+        self._uniform_dx = uniform_dx
         self._create_plan(uniform_dx)
         # dt/eps and dt/mu, the per-cell quotients of the updates, cached on the device and
         # refreshed whenever eps or mu change (tracked through torch's version counter)

@@ -87,6 +87,38 @@ def c3(float_type=numpy.float32, seed: int = 3, shape=(128, 128, 256)):
             "describe": "%dx%dx%d complex (split f32), Bloch x/y, CPML z, eps/mu spheres, PEC sphere" % shape}
 
 
+def c4(n: int = 64, seed: int = 4, steps: int = 2000):
+    """The batched sweep: n L3-cavity variants of the c2 construction (silicon slab eps = 12.11,
+    6 cells thick, triangular lattice of air holes with an L3 defect, 8-cell CPML on all six
+    faces, Ey dipole with the 1550 nm / 20% Gaussian pulse in 40 nm cells, Poynting off) on
+    uneven seeded grids: sx ~ U{96..256}, sy ~ U{96..224}, sz ~ U{48..73}, lattice period
+    a ~ U[8, 12] cells, hole radius r ~ U[0.25a, 0.35a]. Each variant records E_y at its
+    centre every step (the DFT-peak monitor)."""
+    rng = numpy.random.default_rng(seed)
+    dt = 0.99 / math.sqrt(3)
+    wave = geometry.gaussian_pulse(dt, dx_nm=40.0, wavelength_nm=1550.0, bandwidth_nm=0.2 * 1550.0)
+    out = []
+    for v in range(n):
+        shape = (int(rng.integers(96, 257)), int(rng.integers(96, 225)), int(rng.integers(48, 74)))
+        a = float(rng.uniform(8.0, 12.0))
+        r_frac = float(rng.uniform(0.25, 0.35))
+        out.append({"shape": shape, "a": a, "r_frac": r_frac, "seed": int(rng.integers(0, 2 ** 31)),
+                    "steps": steps, "wave": wave})
+    return out
+
+
+def c4_kwargs(var, float_type=numpy.float32):
+    """Simulation keyword arguments and the centre Ey flat index of one c4 variant."""
+    shape = var["shape"]
+    eps = geometry.l3_cavity(shape, a=var["a"], r_frac=var["r_frac"], slab_eps=12.11, slab_thickness=6.0,
+                             jitter_frac=0.01, margin=8, defect_length=3, seed=var["seed"], dtype=float_type)
+    N = int(numpy.prod(shape))
+    centre = tuple(s // 2 for s in shape)
+    index = int(numpy.ravel_multi_index(centre, shape)) + 1 * N
+    kw = dict(epsilon=eps, pmls=c2_pmls(), do_poynting=False, float_type=float_type)
+    return kw, index
+
+
 def face_cells(shape, pmls) -> int:
     """Cells that carry a CPML auxiliary pair, summed over faces (corners count per face)."""
     total = 0
@@ -102,4 +134,4 @@ def face_cells(shape, pmls) -> int:
 
 
 def get(name: str, **kw):
-    return {"c1": c1, "c2": c2, "c3": c3}[name](**kw)
+    return {"c1": c1, "c2": c2, "c3": c3, "c4": c4}[name](**kw)

@@ -61,6 +61,8 @@ STRUCTS = {
     "FdtdDesc": _lib.FdtdDesc,
     "FdtdBuffers": _lib.FdtdBuffers,
     "FdtdPointSources": _lib.FdtdPointSources,
+    "FdtdBatchFace": _lib.FdtdBatchFace,
+    "FdtdBatchVariant": _lib.FdtdBatchVariant,
 }
 
 

@@ -1,0 +1,186 @@
+"""Batched stepping of several variants in one persistent launch (BatchSimulation): float32
+storage is bit-identical to stepping each variant with Simulation.run, for every tile shape,
+through CUDA-graph replays and monitor series; 16-bit storage with per-tile exponents stays
+close to the float32 result and its encode/decode round trip is within the format's rounding."""
+import copy
+import math
+
+import numpy
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from opencl_fdtd_gb300 import geometry  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [((20, 18, 16), 4), ((13, 11, 23), 3), ((9, 25, 7), 2), ((16, 16, 1), 2)]
+
+
+def _variant(shape, T, seed):
+    rng = numpy.random.default_rng(seed)
+    eps = [rng.uniform(1, 6, shape).astype(numpy.float32) for _ in range(3)]
+    eps[0][tuple(slice(1, max(2, s // 4)) for s in shape)] = numpy.inf
+    init = {k: [0.1 * rng.standard_normal(shape).astype(numpy.float32) for _ in range(3)] for k in "EH"}
+    pmls = [{"axis": a, "polarity": p, "thickness": T} for a in "xyz" for p in "np"
+            if 2 * T <= shape["xyz".index(a)]]
+    return dict(epsilon=eps, pmls=pmls, initial_fields=init, do_poynting=False)
+
+
+def _sims(kws):
+    from opencl_fdtd_gb300 import Simulation
+    return [Simulation(**copy.deepcopy(k)) for k in kws]
+
+
+def _sources(sims, nsteps, seed):
+    rng = numpy.random.default_rng(seed)
+    out = []
+    for s in sims:
+        out.append([(int(rng.integers(0, 3 * s.N)), [math.sin(0.2 * t + k) for t in range(nsteps)])
+                    for k in range(2)])
+    return out
+
+
+def _monitors(sims, seed):
+    rng = numpy.random.default_rng(seed)
+    return [[int(rng.integers(0, 3 * s.N)) for _ in range(3)] for s in sims]
+
+
+def _same(a, b):
+    for k in ("E", "H"):
+        x, y = getattr(a, k), getattr(b, k)
+        assert torch.equal(x, y), (k, int((x != y).sum()))
+    for fld in "EH":
+        for (u1, v1), (u2, v2) in zip(a.psi[fld], b.psi[fld]):
+            assert torch.equal(u1, u2) and torch.equal(v1, v2), fld
+
+
+@pytest.mark.parametrize("tiles", [(8, 0, "launches"), (1, 0, "launches"), (8, 0, "persistent"),
+                                   (1, 1, "persistent"), (3, 2, "persistent"), (64, 0, "launches")])
+def test_batch_f32_equals_per_variant_runs(tiles):
+    from opencl_fdtd_gb300.batch import BatchSimulation
+    kws = [_variant(s, T, 10 + i) for i, (s, T) in enumerate(SHAPES)]
+    n = 9
+    ref = _sims(kws)
+    got = _sims(kws)
+    src = _sources(ref, n, 5)
+    mon = _monitors(ref, 6)
+    series_ref = []
+    for sim, ps, ms in zip(ref, src, mon):
+        m = sim.dft_monitor([(i // sim.N, numpy.unravel_index(i % sim.N, sim.shape)) for i in ms], ())
+        sim.run(n, point_sources=ps, monitor=m, path="plain")
+        series_ref.append(m.series())
+    b = BatchSimulation(got, storage="f32", sources=src, monitors=mon, steps=n)
+    b.tune(*tiles)
+    b.run(4)
+    b.run(5)
+    torch.cuda.synchronize()
+    assert b.step_counter() == n
+    for r, g, sr, sg in zip(ref, got, series_ref, b.series):
+        _same(r, g)
+        assert numpy.array_equal(sr, sg.cpu().numpy())
+
+
+def test_batch_graph_replay_equals_run():
+    from opencl_fdtd_gb300.batch import BatchSimulation
+    kws = [_variant(s, T, 30 + i) for i, (s, T) in enumerate(SHAPES[:3])]
+    a_s, b_s = _sims(kws), _sims(kws)
+    src = _sources(a_s, 12, 7)
+    a = BatchSimulation(a_s, sources=src, steps=12)
+    b = BatchSimulation(b_s, sources=src, steps=12)
+    a.tune(8, 0, "persistent")
+    a.run(12)
+    b.capture(4)
+    for _ in range(3):
+        b.replay()
+    torch.cuda.synchronize()
+    assert b.step_counter() == 12
+    for x, y in zip(a_s, b_s):
+        _same(x, y)
+
+
+@pytest.mark.parametrize("storage,tol", [("bf16", 5e-2), ("fp16", 1e-2)])
+def test_batch_16bit_storage_tracks_f32(storage, tol):
+    from opencl_fdtd_gb300.batch import BatchSimulation
+    kws = [_variant(s, T, 50 + i) for i, (s, T) in enumerate(SHAPES[:3])]
+    ref, got = _sims(kws), _sims(kws)
+    src = _sources(ref, 20, 8)
+    BatchSimulation(ref, storage="f32", sources=src, steps=20).run(20)
+    b = BatchSimulation(got, storage=storage, sources=src, steps=20)
+    b.run(20)
+    b.sync()
+    torch.cuda.synchronize()
+    for r, g in zip(ref, got):
+        for k in ("E", "H"):
+            x = getattr(r, k).double()
+            y = getattr(g, k).double()
+            fin = torch.isfinite(x)
+            err = torch.linalg.norm((x - y)[fin]) / torch.linalg.norm(x[fin])
+            assert err < tol, (storage, k, float(err))
+
+
+@pytest.mark.parametrize("storage,bits", [("bf16", 8), ("fp16", 11)])
+def test_batch_encode_decode_round_trip(storage, bits):
+    """Per-tile exponents keep every tile at full 16-bit precision, whatever its level: tiles
+    whose values span 1e-30 .. 1e3 decode within half an ulp of the format."""
+    from opencl_fdtd_gb300 import Simulation
+    from opencl_fdtd_gb300.batch import BatchSimulation
+    shape = (6, 20, 40)
+    sim = Simulation(epsilon=[numpy.ones(shape, numpy.float32)] * 3, pmls=[], do_poynting=False)
+    rng = numpy.random.default_rng(3)
+    N = sim.N
+    levels = 10.0 ** rng.uniform(-30, 3, size=3 * N)
+    vals = (rng.standard_normal(3 * N) * levels).astype(numpy.float32)
+    sim.E.copy_(torch.from_numpy(vals))
+    b = BatchSimulation([sim], storage=storage)
+    sim.E.zero_()
+    b.sync()
+    torch.cuda.synchronize()
+    got = sim.E.cpu().numpy().astype(numpy.float64)
+    want = vals.astype(numpy.float64)
+    # within a tile (32 cells) the step is 2^-bits of the tile's largest magnitude
+    syz = shape[1] * shape[2]
+    for c in range(3):
+        for x in range(shape[0]):
+            for jt in range((syz + 31) // 32):
+                lo = c * N + x * syz + jt * 32
+                hi = min(lo + 32, c * N + (x + 1) * syz)
+                m = numpy.abs(want[lo:hi]).max()
+                assert numpy.abs(got[lo:hi] - want[lo:hi]).max() <= m * 2.0 ** (-bits)
+
+
+def test_batch_rejects_unsupported_simulations():
+    from opencl_fdtd_gb300 import Simulation
+    from opencl_fdtd_gb300.batch import BatchSimulation
+    shape = (10, 10, 10)
+    eps, mu = geometry.sphere_inclusions(shape, n=2, rmin=2, rmax=3, seed=1)
+    with pytest.raises(ValueError):
+        BatchSimulation([Simulation(epsilon=eps, mu=mu, pmls=[], do_poynting=False)])
+    with pytest.raises(ValueError):
+        BatchSimulation([Simulation(epsilon=eps, pmls=[], do_poynting=True)])
+    with pytest.raises(ValueError):
+        BatchSimulation([Simulation(epsilon=eps, pmls=[], do_poynting=False)], storage="int8")
+
+
+def test_autotune_restores_state_and_caches(tmp_path):
+    from opencl_fdtd_gb300.batch import BatchSimulation
+    kws = [_variant(s, T, 70 + i) for i, (s, T) in enumerate(SHAPES[:3])]
+    a_s, b_s = _sims(kws), _sims(kws)
+    src = _sources(a_s, 8, 9)
+    mon = _monitors(a_s, 10)
+    a = BatchSimulation(a_s, sources=src, monitors=mon, steps=8)
+    b = BatchSimulation(b_s, sources=src, monitors=mon, steps=8)
+    a.run(3)
+    b.run(3)
+    cache = str(tmp_path / "tune.json")
+    choice = b.autotune(steps=2, cache_path=cache, xchunks=(2, 8), blocks=(1, 2))
+    assert not choice["cached"] and len(choice["timings"]) == 6
+    assert b.step_counter() == 3
+    a.run(5)
+    b.run(5)
+    torch.cuda.synchronize()
+    for x, y, sa, sb in zip(a_s, b_s, a.series, b.series):
+        _same(x, y)
+        assert torch.equal(sa, sb)
+    again = b.autotune(steps=2, cache_path=cache, xchunks=(2, 8), blocks=(1, 2))
+    assert again["cached"] and again["xchunk"] == choice["xchunk"]
