@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--c4-variants", type=int, default=64, help="c4: number of cavity variants")
     ap.add_argument("--c4-steps", type=int, default=2000, help="c4: steps of every variant")
     ap.add_argument("--c4-chunk", type=int, default=100, help="c4: steps per captured launch")
+    ap.add_argument("--c5-runs", type=int, default=200, help="c5: teacher runs at 128^3")
+    ap.add_argument("--c5-steps", type=int, default=2000, help="c5: timed steps of the c2 cavity forms")
     ap.add_argument("--path", choices=["fused", "slab", "hs", "dropin", "default", "all"], default="default",
                     help="default = per-call loop (per-kernel timing) + Simulation.run (hs path); "
                          "slab = run over the per-update kernels; fused = the opt-in fused step")
@@ -693,9 +695,163 @@ def run_c4(args):
     print(json.dumps(line), flush=True)
 
 
+def run_c5(args):
+    """Learned thin boundary on the c2 cavity: train the boundary network (teacher runs, ridge
+    least-squares start, Adam fine-tune, all on the device), judge it (reflection against a
+    doubled grid, long-run stability), then time the c2 cavity (a) plain with its 8-cell CPML
+    (395x345x73) and (b) cut to its useful interior plus a 2-cell learned layer per face
+    (383x333x61), and report the form the judge deploys. Throughput counts useful-interior
+    cells (379x329x57 in both forms)."""
+    import torch
+    from opencl_fdtd_gb300 import Simulation, workloads
+    from opencl_fdtd_gb300 import learned_boundary as L
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    net, data, start, fin = L.train(runs=args.c5_runs, seed=5)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    tvar = {f: float(((data.T[f] ** 2) * net.output_weights(f)).mean()) for f in range(6)}
+    rel = {"start": [round(start[f] / tvar[f], 5) for f in range(6)],
+           "finetuned": [round(fin[f] / tvar[f], 5) for f in range(6)]}
+    samples = data.sizes()
+    del data
+    torch.cuda.empty_cache()
+    lb = L.LearnedBoundary(net, "bf16")
+    t0 = time.perf_counter()
+    verdict = L.judge(lb)
+    judge_s = time.perf_counter() - t0
+    zero = L.BoundaryNet(seed=3)
+    zero.params.zero_()
+    held = L.reflection_db(L.LearnedBoundary(zero, "bf16"), shape=(96, 96, 96), steps=400, period=20.0)
+    first_pass = L.reflection_db(lb, shape=(96, 96, 96), steps=250, period=20.0)
+    held_first = L.reflection_db(L.LearnedBoundary(zero, "bf16"), shape=(96, 96, 96), steps=250, period=20.0)
+
+    # the c2 cavity: plain with its CPML, and cut to the useful interior plus the 2-cell layer
+    K = args.c5_steps
+    wl = workloads.c2()
+    kw = dict(wl["kwargs"])
+    shape = wl["shape"]
+    thin_off = 8 - 2
+    thin_shape = tuple(s_ - 2 * thin_off for s_ in shape)
+    useful = tuple(s_ - 16 for s_ in shape)
+    useful_cells = int(numpy.prod(useful))
+    wave = [wl["wave"](t) for t in range(K)]
+
+    def timed(sim, ind):
+        sim.run(3, point_sources=[(ind, wave[:3])])
+        for t_ in (sim.E, sim.H):
+            t_.zero_()
+        if sim.do_poynting:
+            sim.S.zero_()
+        for f_ in ("E", "H"):
+            for u, v in sim.psi[f_]:
+                u.zero_()
+                v.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(sim.queue)
+        sim.run(K, point_sources=[(ind, wave)])
+        e1.record(sim.queue)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    plain = Simulation(**kw)
+    ms_plain = timed(plain, wl["source_index"])
+    Ep = plain.E.view(3, *shape)[:, 8:8 + useful[0], 8:8 + useful[1], 8:8 + useful[2]].clone()
+    plain.close()
+    del plain
+    sl = tuple(slice(thin_off, thin_off + n) for n in thin_shape)
+    kw_thin = dict(kw)
+    kw_thin["epsilon"] = [numpy.ascontiguousarray(e[sl]) for e in kw["epsilon"]]
+    kw_thin["pmls"] = []
+    kw_thin["dt"] = L.DEFAULT_DT
+    thin = Simulation(**kw_thin)
+    lb.attach(thin)
+    c = numpy.unravel_index(wl["source_index"] % int(numpy.prod(shape)), shape)
+    comp = wl["source_index"] // int(numpy.prod(shape))
+    ind_thin = comp * thin.N + int(numpy.ravel_multi_index(tuple(ci - thin_off for ci in c), thin_shape))
+    ms_thin = timed(thin, ind_thin)
+    Et = thin.E.view(3, *thin_shape)[:, 2:2 + useful[0], 2:2 + useful[1], 2:2 + useful[2]]
+    finite = bool(torch.isfinite(Et).all())
+    l2 = float(torch.linalg.norm((Et - Ep).double()) / torch.linalg.norm(Ep.double())) if finite else float("inf")
+    # the network's share of a thin step: one predict launch per step, timed alone
+    n_cols, _ = L.columns(thin_shape)
+    W = net.weights("bf16")
+    pred = torch.empty(n_cols * 6, dtype=torch.float32, device="cuda")
+    lib = L._lib.load()
+
+    def predict():
+        L._lib.check(lib.fdtd_lbc_predict(L._shape_arg(thin_shape), 63, -1, L.PRECISIONS["bf16"], W.data_ptr(),
+                                          thin.E.data_ptr(), thin.H.data_ptr(), pred.data_ptr(), pred.numel(),
+                                          ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    thin.E.zero_()
+    thin.H.zero_()
+    for _ in range(3):
+        predict()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(50):
+        predict()
+    e1.record()
+    e1.synchronize()
+    ms_pred = e0.elapsed_time(e1) / 50
+    flops = 2.0 * (108 * 64 + 64 * 64 + 64 * 6) * n_cols
+    peaks = {}
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except (OSError, ValueError):
+        pass
+    tc_peak = float(peaks.get("bf16_tflops", 1900.0))
+    lb.detach(thin)
+    thin.close()
+
+    deployed = "learned" if verdict["accepted"] else "cpml"
+    v_plain = useful_cells * K / (ms_plain * 1e-3) / 1e6
+    v_thin = useful_cells * K / (ms_thin * 1e-3) / 1e6
+    value = v_thin if deployed == "learned" else v_plain
+    line = {
+        "metric": METRIC + " (useful interior)", "value": round(value, 2), "unit": UNIT, "n_gpus": 1, "steps": K,
+        "warmup": 3, "ms_per_step": round((ms_thin if deployed == "learned" else ms_plain) / K, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 fields; boundary MLP bf16 weights, f32 accumulation", "data": "synthetic (seeded)",
+        "config": {"workload": "c5: c2 cavity %s, useful interior %s; 2-cell learned layer (%s grid) or "
+                               "8-cell CPML; Poynting on; %d steps" % ("x".join(map(str, shape)),
+                                                                      "x".join(map(str, useful)),
+                                                                      "x".join(map(str, thin_shape)), K),
+                   "teacher": "%d runs at 128^3, 16-cell CPML, 1500 steps, 1-8 spheres eps U[1,12] inside "
+                              "the box, dipole pulse period U[10,30] steps, random polarisation" % args.c5_runs,
+                   "l2": "c2 fields (%.0f MB) larger than the 129 MB L2; no flush" % (int(numpy.prod(shape)) * 36 / 1e6)},
+        "deployed": deployed,
+        "verdict": {k: (round(v, 2) if isinstance(v, float) and math.isfinite(v) else v) for k, v in verdict.items()
+                    if k != "reflection_by_period"},
+        "reflection_by_period_db": {str(k): round(v, 2) for k, v in verdict["reflection_by_period"].items()},
+        "first_pass_reflection_db": {"learned": round(first_pass["reflection_db"], 2),
+                                     "zero_ghost_layer": round(held_first["reflection_db"], 2)},
+        "zero_ghost_layer_reflection_db": round(held["reflection_db"], 2),
+        "training": {"seconds": round(train_s, 1), "samples_per_face": samples, "relative_loss": rel},
+        "judge_seconds": round(judge_s, 1),
+        "plain_cpml8": {"ms": round(ms_plain, 3), "useful_mcells_per_s": round(v_plain, 2),
+                        "grid": list(shape)},
+        "thin_learned": {"ms": round(ms_thin, 3), "useful_mcells_per_s": round(v_thin, 2), "grid": list(thin_shape),
+                         "finite_after_steps": finite,
+                         "interior_rel_l2_vs_plain_cpml8": l2 if math.isfinite(l2) else "inf",
+                         "predict_ms_per_step": round(ms_pred, 4), "boundary_columns": n_cols},
+        "roofline": {"bound": "tensor", "achieved": round(flops / (ms_pred * 1e-3) / 1e12, 2),
+                     "peak": tc_peak, "unit": "TFLOP/s", "frac": round(flops / (ms_pred * 1e-3) / 1e12 / tc_peak, 4),
+                     "traffic": None, "kernel": "k_lbc_predict_mma (bf16 mma.sync)"},
+        "gpu_launches": "thin: 4 + the plain step's per step; plain: the plain step's",
+    }
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     _a = parse()
     if _a.workload == "c4" and _a.impl == "ours":
         run_c4(_a)
+    elif _a.workload == "c5" and _a.impl == "ours":
+        run_c5(_a)
     else:
         main()

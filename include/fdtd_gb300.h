@@ -294,6 +294,80 @@ int fdtd_batch_set_step(FdtdBatch *batch, int64_t step);
 int fdtd_batch_encode(FdtdBatch *batch, int32_t v, int32_t field, const float *src, void *stream);
 int fdtd_batch_decode(FdtdBatch *batch, int32_t v, int32_t field, float *dst, void *stream);
 
+/* ---- learned thin absorbing boundary ------------------------------------------------------
+ * Replaces the CPML of selected faces (bit 2 * axis + side of face_mask; side 0 = index 0) by
+ * a per-face MLP. Every column of a face (one cell of the face's plane) reads the six field
+ * components (Ex Ey Ez Hx Hy Hz) on a 3 x 3 tangential patch two cells deep,
+ * [depth][du + 1][dv + 1][component], with tangential neighbours past the grid clamped to its
+ * edge. x = stencil / r with r its RMS; the network 108 -> 64 -> 64 -> 6 (GELU) maps x to the
+ * six components of the ghost cell one step outside the face, divided by r. The grid's edges wrap; a boundary step is: the ghosts of every face from the
+ * pre-step state E^n, H^{n+1/2} (H^{n+1/2} outside side-0 faces, E^{n+1} outside side-1
+ * faces); E update; E fix-up; sources; H update; H fix-up (fdtd_lbc_fix). Edge cells get one
+ * term per face they lie on.
+ * Parameters: float32 [LBC_NPARAM] per face, W1 [108][64], b1 [64], W2 [64][64], b2 [64],
+ * W3 [64][6], b3 [6] (row-major [in][out]); 6 faces in order 2 * axis + side. No reference
+ * interface is replaced: opencl_fdtd absorbs only with CPML (simulation.py:274-319). */
+#define FDTD_LBC_IN 108
+#define FDTD_LBC_HID 64
+#define FDTD_LBC_OUT 6
+#define FDTD_LBC_NPARAM 11526
+#define FDTD_LBC_PACK_WORDS 6024   /* bfloat16 tensor-core layout of one face, 32-bit words */
+#define FDTD_LBC_F32 0              /* float32 weights, CUDA cores */
+#define FDTD_LBC_BF16 1             /* bfloat16 weights and activations, tensor cores */
+#define FDTD_LBC_BF16X2 2           /* bfloat16 weights, activations as two bfloat16 parts */
+
+/* Columns of the faces in face_mask (whole planes); face_offsets[f] (f = 2 * axis + side) is
+ * the first column of face f (-1 when absent), face_offsets[6] the total. face_offsets may be
+ * NULL. Columns of a face run over its plane row-major in (u, v), the other axes in xyz order. */
+int fdtd_lbc_columns(const int32_t shape[3], int32_t face_mask, int32_t *ncol, int32_t face_offsets[7]);
+/* Training data of one state: X [ncol][108] = stencil / r, R [ncol] = r, C [ncol][6] = the
+ * outermost cell's components (any of X, R, C may be NULL). */
+int fdtd_lbc_gather(const int32_t shape[3], int32_t face_mask, const float *E, const float *H, float *X,
+                    float *R, float *C, void *stream);
+/* Training, float32, one network: forward of a batch keeps the pre-activations A1, A2 and
+ * activations H1, H2 ([batch][64] each); backward gives the gradient of the mean over
+ * batch x 6 of w_o (Y - T)^2 (out_weights: 6 device floats w_o, NULL = all 1) with respect to
+ * the parameters (grad [LBC_NPARAM]), deterministic for a given batch; workspace floats from
+ * fdtd_mlp_backward_workspace. */
+int fdtd_mlp_forward(const float *params, const float *X, int32_t batch, float *Y, float *A1, float *A2,
+                     float *H1, float *H2, void *stream);
+int fdtd_mlp_backward_workspace(int32_t batch, int64_t *floats);
+int fdtd_mlp_backward(const float *params, const float *X, const float *Y, const float *T,
+                      const float *out_weights, int32_t batch, const float *A1, const float *A2, const float *H1,
+                      const float *H2, float *grad, float *workspace, int64_t workspace_floats, void *stream);
+/* out [(K + 1) x N] float32: A^T B in rows 0..K-1 and the column sums of B in row K, for
+ * A [rows][K], B [rows][N] (the least-squares normal equations of the linear start of
+ * training); deterministic (fixed partition of the rows, fixed folding order). (K + 1) N <=
+ * 7168. Workspace floats from fdtd_gram_workspace. */
+int fdtd_gram_workspace(int32_t rows, int32_t K, int32_t N, int64_t *floats);
+int fdtd_gram(const float *A, int32_t rows, int32_t K, const float *B, int32_t N, float *out, float *workspace,
+              int64_t workspace_floats, void *stream);
+/* One Adam step (Kingma and Ba 2015, bias-corrected; step counts from 1) on n parameters. */
+int fdtd_adam(float *params, const float *grad, float *m, float *v, int32_t n, float lr, float beta1,
+              float beta2, float eps, int32_t step, void *stream);
+/* float32 parameters [6][LBC_NPARAM] -> bfloat16 tensor-core layout [6][LBC_PACK_WORDS]. */
+int fdtd_lbc_pack(const float *params, void *packed, void *stream);
+/* Ghost values [ncol][6] (r times the network output) of the faces of side `side` (-1: all);
+ * weights: float32 parameters (FDTD_LBC_F32) or the packed layout (BF16, BF16X2). */
+int fdtd_lbc_predict(const int32_t shape[3], int32_t face_mask, int32_t side, int32_t precision,
+                     const void *weights, const float *E, const float *H, float *pred, int64_t pred_floats,
+                     void *stream);
+/* Replace, in the updates of the outermost cells, the wrapped neighbour by the ghost:
+ * FDTD_LBC_FIX_E right after the E update, E_q += -e_qap ce_q (ghost H_p - wrapped H_p) for
+ * every learned side-0 face of axis a through the cell (q, a, p distinct, e the Levi-Civita
+ * sign, ce = dt / eps: 3N floats); FDTD_LBC_FIX_H after the H update, H_q += -e_qap ch_q
+ * (ghost E_p - wrapped E_p) for every learned side-1 face (ch = cm, 3N floats dt / mu, or dt
+ * when cm is NULL). Unit cells. One of the two per call. */
+#define FDTD_LBC_FIX_E 1
+#define FDTD_LBC_FIX_H 2
+int fdtd_lbc_fix(const int32_t shape[3], int32_t face_mask, int32_t fields, const float *pred, float *E, float *H,
+                 const float *ce, const float *cm, double dt, void *stream);
+/* Make fdtd_run step the plan with the learned boundary (float32 plans with unit cells and no
+ * Bloch boundaries; face_mask 0 detaches). weights and pred (ncol x 6 floats) stay owned by
+ * the caller and must outlive the attachment. The faces in face_mask should carry no CPML. */
+int fdtd_lbc_attach(FdtdPlan *plan, int32_t face_mask, int32_t precision, const void *weights, float *pred,
+                    int64_t pred_floats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -122,7 +122,32 @@ SIGNATURES = [
     ("fdtd_batch_set_step", c_i32, [c_vp, c_i64]),
     ("fdtd_batch_encode", c_i32, [c_vp, c_i32, c_i32, c_vp, c_vp]),
     ("fdtd_batch_decode", c_i32, [c_vp, c_i32, c_i32, c_vp, c_vp]),
+    ("fdtd_lbc_columns", c_i32, [_P(c_i32), c_i32, _P(c_i32), _P(c_i32)]),
+    ("fdtd_lbc_gather", c_i32, [_P(c_i32), c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    ("fdtd_mlp_forward", c_i32, [c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    ("fdtd_mlp_backward_workspace", c_i32, [c_i32, _P(c_i64)]),
+    ("fdtd_mlp_backward", c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                  c_i64, c_vp]),
+    ("fdtd_gram_workspace", c_i32, [c_i32, c_i32, c_i32, _P(c_i64)]),
+    ("fdtd_gram", c_i32, [c_vp, c_i32, c_i32, c_vp, c_i32, c_vp, c_vp, c_i64, c_vp]),
+    ("fdtd_adam", c_i32, [c_vp, c_vp, c_vp, c_vp, c_i32, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                          ctypes.c_float, c_i32, c_vp]),
+    ("fdtd_lbc_pack", c_i32, [c_vp, c_vp, c_vp]),
+    ("fdtd_lbc_predict", c_i32, [_P(c_i32), c_i32, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    ("fdtd_lbc_fix", c_i32, [_P(c_i32), c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_f64, c_vp]),
+    ("fdtd_lbc_attach", c_i32, [c_vp, c_i32, c_i32, c_vp, c_vp, c_i64]),
 ]
+
+FDTD_LBC_IN = 108
+FDTD_LBC_HID = 64
+FDTD_LBC_OUT = 6
+FDTD_LBC_NPARAM = 11526
+FDTD_LBC_PACK_WORDS = 6024
+FDTD_LBC_FIX_E = 1
+FDTD_LBC_FIX_H = 2
+FDTD_LBC_F32 = 0
+FDTD_LBC_BF16 = 1
+FDTD_LBC_BF16X2 = 2
 
 _LIB = None
 _LOCK = threading.Lock()

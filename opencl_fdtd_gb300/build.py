@@ -34,6 +34,8 @@ UNITS = {
     "hs_fused.cu": ["--fmad=false"],
     "batch.cu": ["--fmad=false"],
     "batch_abi.cu": [],
+    "lbc.cu": [],
+    "lbc_abi.cu": [],
     "monitors.cu": [],
     "noalloc.cu": [],
     "fdtd_abi.cu": [],

@@ -386,9 +386,11 @@ int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
     for (int t = 0; t < nsteps; ++t) {
         const int a = t & 1, o = a ^ 1;
         bb.H = H[a];
+        if ((rc = lbc_before_e(p, b, H[a], st))) return rc;
         if ((rc = timer.mark(t, 0))) return rc;
         if ((rc = run_update_e<R>(p, &bb, st, false))) return rc;
         if ((rc = timer.mark(t, 1))) return rc;
+        if ((rc = lbc_after_e(p, b, H[a], st))) return rc;
         if (src && src->n > 0 && (rc = run_point_sources<R>(p, &bb, st, src, t))) return rc;
         k.E = (const R *)b->E;
         k.HA = (const R *)H[a];
@@ -408,6 +410,7 @@ int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
         if ((rc = timer.mark(t, 2))) return rc;
         if ((rc = check_cuda(launch_hs<R>(k, p->d.has_mu != 0, dxmode, p->hs_prefetch != 0, st), "H+S launch"))) return rc;
         if ((rc = timer.mark(t, 3))) return rc;
+        if ((rc = lbc_after_h(p, b, H[o], st))) return rc;
         if (mon && (rc = run_dft<R>(p, b->E, st, mon, t))) return rc;
     }
     if ((rc = timer.finish())) return rc;
@@ -436,17 +439,21 @@ int run_slabs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
               const FdtdPointSources *src, const FdtdDftMonitor *mon)
 {
     const uint32_t sx = p->sx;
-    const uint32_t W = p->slab ? p->slab : sx;
+    // the learned boundary's E corrections must land before any H update reads them: whole grid
+    const uint32_t W = p->slab && !p->lbc_mask ? p->slab : sx;
     const bool bloch = p->d.n_bloch != 0, poynt = p->d.do_poynting != 0;
     int rc;
     if (W >= sx) {
         // one slab: the plain whole-grid sequence
         for (int t = 0; t < nsteps; ++t) {
+            if ((rc = lbc_before_e(p, b, b->H, st))) return rc;
             if ((rc = run_update_e<R>(p, b, st, false))) return rc;
             if (bloch && (rc = run_update_e<R>(p, b, st, true))) return rc;
+            if ((rc = lbc_after_e(p, b, b->H, st))) return rc;
             if (src && src->n > 0 && (rc = run_point_sources<R>(p, b, st, src, t))) return rc;
             if ((rc = run_update_h<R>(p, b, st, false))) return rc;
             if (bloch && (rc = run_update_h<R>(p, b, st, true))) return rc;
+            if ((rc = lbc_after_h(p, b, b->H, st))) return rc;
             if (poynt && (rc = run_update_s<R>(p, b, st))) return rc;
             if (mon && (rc = run_dft<R>(p, b->E, st, mon, t))) return rc;
         }
@@ -1042,7 +1049,7 @@ int fdtd_run(FdtdPlan *p, const FdtdBuffers *b, void *stream, int32_t nsteps,
         if (!rc && mon) { mon->step += nsteps; mon->series_row += nsteps; }
         return rc;
     }
-    if (fused_eligible(p, b, src)) {
+    if (!p->lbc_mask && fused_eligible(p, b, src)) {
         if ((rc = check_psi(p, b->psi_e, "fdtd_run")) || (rc = check_psi(p, b->psi_h, "fdtd_run")))
             return rc;
         cudaStream_t st = (cudaStream_t)stream;

@@ -23,9 +23,20 @@ struct FdtdPlan {
     int32_t kernel_samples;     // launches each mean is over
     void *coef = nullptr;       // device copy of every face's six coefficient tables
     const void *tab[6][6];      // per face: p0e p1e p2e p0h p1h p2h (device pointers)
+    // learned boundary attached with fdtd_lbc_attach (lbc_mask 0: none)
+    int32_t lbc_mask = 0;       // faces, bit 2 * axis + side
+    int32_t lbc_precision = 0;  // FDTD_LBC_F32 / BF16 / BF16X2
+    const void *lbc_w = nullptr;
+    float *lbc_pred = nullptr;  // [columns][6] predictions of the current step
 };
 
 namespace fdtd {
 int set_error(int code, const char *msg);
 int check_cuda(cudaError_t e, const char *what);
+// learned boundary around one step (no-ops when none is attached; lbc_abi.cu): the ghosts of
+// every face from the pre-step state, the E fix-up after the E update, the H fix-up after the
+// H update
+int lbc_before_e(const FdtdPlan *p, const FdtdBuffers *b, const void *H, cudaStream_t st);
+int lbc_after_e(const FdtdPlan *p, const FdtdBuffers *b, const void *H, cudaStream_t st);
+int lbc_after_h(const FdtdPlan *p, const FdtdBuffers *b, void *H, cudaStream_t st);
 }  // namespace fdtd

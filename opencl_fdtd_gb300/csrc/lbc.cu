@@ -1,0 +1,784 @@
+// Learned thin absorbing boundary: stencil gather, the boundary MLP's training kernels
+// (forward, backward, Adam), its inference kernels and the boundary fix-up of the Yee updates.
+//
+// The boundary model: on every face with the learned layer, each column (one cell of the face's
+// plane) reads the six field components on a 3 x 3 tangential patch two cells deep, scales
+// them by their RMS r (Maxwell's equations are linear, so scaling the fields by a scales the
+// answer by a: dividing by r makes the network's job amplitude-free), and a 108 -> 64 -> 64 -> 6
+// MLP with GELU returns the fields of the ghost cell just outside the face, times r. The grid's
+// own edges wrap; the fix-up replaces, in the updates of the outermost cells, the wrapped
+// neighbour by the ghost (H ghosts outside side-0 faces for the E update, E ghosts outside
+// side-1 faces for the H update), which is what a wave leaving the grid needs from the CPML
+// layers that the learned layer replaces.
+//
+// Training runs in float32 with one thread per sample for the per-sample passes (weights in
+// shared memory, broadcast reads) and a split reduction over samples for the weight gradients
+// (deterministic: fixed partition, fixed folding order). Inference uses bfloat16 weights on
+// the tensor cores (mma.sync, float32 accumulation) or float32 weights on the CUDA cores.
+#include <cuda_bf16.h>
+
+#include "lbc.h"
+
+namespace fdtd {
+
+namespace {
+
+constexpr int T_FWD = 128;
+constexpr int WG_ROWS = 32;      // rows staged per pass of the weight-gradient kernel
+constexpr int WG_THREADS = 256;
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+
+__device__ __forceinline__ float gelu_d(float x)
+{
+    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+
+__device__ __forceinline__ uint32_t clampu(int v, uint32_t n) { return (uint32_t)(v < 0 ? 0 : (v >= (int)n ? (int)n - 1 : v)); }
+
+// cell coordinates of column (u, v) of face f at depth d with tangential offset (du, dv)
+__device__ __forceinline__ uint64_t cell_of(const LGrid &g, const LFace &f, uint32_t u, uint32_t v, int d,
+                                            int du, int dv)
+{
+    const int a = f.axis, ua = a == 0 ? 1 : 0, va = a == 2 ? 1 : 2;
+    uint32_t c[3];
+    c[a] = f.side ? g.s[a] - 1u - (uint32_t)d : (uint32_t)d;
+    c[ua] = clampu((int)u + du, g.s[ua]);
+    c[va] = clampu((int)v + dv, g.s[va]);
+    return ((uint64_t)c[0] * g.s[1] + c[1]) * g.s[2] + c[2];
+}
+
+__device__ __forceinline__ int face_of(const LGrid &g, uint32_t col)
+{
+    int f = 0;
+    while (f + 1 < g.nface && col >= g.face[f + 1].col0) ++f;
+    return f;
+}
+
+// the 108 stencil values of a column; returns their RMS
+__device__ __forceinline__ float gather(const LGrid &g, const LFace &f, uint32_t u, uint32_t v, const float *E,
+                                        const float *H, float *x)
+{
+    float ss = 0.f;
+    int k = 0;
+#pragma unroll
+    for (int d = 0; d < 2; ++d)
+#pragma unroll
+        for (int du = -1; du <= 1; ++du)
+#pragma unroll
+            for (int dv = -1; dv <= 1; ++dv) {
+                const uint64_t i = cell_of(g, f, u, v, d, du, dv);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float e = E[c * g.N + i], h = H[c * g.N + i];
+                    x[k + c] = e;
+                    x[k + 3 + c] = h;
+                    ss += e * e + h * h;
+                }
+                k += 6;
+            }
+    return sqrtf(ss * (1.0f / LBC_IN));
+}
+
+// ---- stencil gather: normalised inputs, their scale, the depth-0 centre values -----------------
+__global__ void k_lbc_gather(const LGrid g, const float *E, const float *H, float *X, float *R, float *C)
+{
+    const uint32_t col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= g.ncol) return;
+    const LFace &f = g.face[face_of(g, col)];
+    const uint32_t c = col - f.col0;
+    const uint32_t u = f.u0 + c / f.nv, v = f.v0 + c % f.nv;
+    float x[LBC_IN];
+    const float r = gather(g, f, u, v, E, H, x);
+    const float inv = r > 0.f ? 1.0f / r : 0.f;
+    if (X)
+        for (int k = 0; k < LBC_IN; ++k) X[(uint64_t)col * LBC_IN + k] = x[k] * inv;
+    if (R) R[col] = r;
+    if (C) {
+        // depth 0, du = dv = 0: stencil entry ((0 * 3 + 1) * 3 + 1) * 6
+        for (int k = 0; k < LBC_OUT; ++k) C[(uint64_t)col * LBC_OUT + k] = x[24 + k];
+    }
+}
+
+// ---- training: forward (float32), one thread per sample ---------------------------------------
+__global__ void __launch_bounds__(T_FWD) k_mlp_fwd(const float *P, const float *X, int B, float *Y, float *A1,
+                                                    float *A2, float *H1, float *H2)
+{
+    __shared__ float w[LBC_NPARAM];
+    for (int i = threadIdx.x; i < LBC_NPARAM; i += blockDim.x) w[i] = P[i];
+    __syncthreads();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= B) return;
+    float h[LBC_HID], a[LBC_HID];
+#pragma unroll
+    for (int j = 0; j < LBC_HID; ++j) a[j] = w[LBC_B1 + j];
+    for (int k = 0; k < LBC_IN; ++k) {
+        const float xk = X[(uint64_t)r * LBC_IN + k];
+#pragma unroll
+        for (int j = 0; j < LBC_HID; ++j) a[j] += xk * w[LBC_W1 + k * LBC_HID + j];
+    }
+#pragma unroll
+    for (int j = 0; j < LBC_HID; ++j) {
+        A1[(uint64_t)r * LBC_HID + j] = a[j];
+        h[j] = gelu(a[j]);
+        H1[(uint64_t)r * LBC_HID + j] = h[j];
+    }
+#pragma unroll
+    for (int j = 0; j < LBC_HID; ++j) a[j] = w[LBC_B2 + j];
+#pragma unroll
+    for (int k = 0; k < LBC_HID; ++k) {
+        const float hk = h[k];
+#pragma unroll
+        for (int j = 0; j < LBC_HID; ++j) a[j] += hk * w[LBC_W2 + k * LBC_HID + j];
+    }
+#pragma unroll
+    for (int j = 0; j < LBC_HID; ++j) {
+        A2[(uint64_t)r * LBC_HID + j] = a[j];
+        h[j] = gelu(a[j]);
+        H2[(uint64_t)r * LBC_HID + j] = h[j];
+    }
+#pragma unroll
+    for (int o = 0; o < LBC_OUT; ++o) {
+        float y = w[LBC_B3 + o];
+#pragma unroll
+        for (int k = 0; k < LBC_HID; ++k) y += h[k] * w[LBC_W3 + k * LBC_OUT + o];
+        Y[(uint64_t)r * LBC_OUT + o] = y;
+    }
+}
+
+// ---- training: backward through the activations, one thread per sample ------------------------
+// loss = scale * sum over the batch and the outputs of w_o (Y - T)^2 (scale = 1 / (B * 6) for the
+// mean, w_o = 1 without wout): DY, and the pre-activation gradients D2 (layer 2) and D1 (layer 1)
+__global__ void __launch_bounds__(T_FWD) k_mlp_bwd_rows(const float *P, const float *Y, const float *T,
+                                                         const float *wout, int B, float scale, const float *A1,
+                                                         const float *A2, float *DY, float *D2, float *D1)
+{
+    __shared__ float w[LBC_NPARAM];
+    for (int i = threadIdx.x; i < LBC_NPARAM; i += blockDim.x) w[i] = P[i];
+    __syncthreads();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= B) return;
+    float dy[LBC_OUT];
+#pragma unroll
+    for (int o = 0; o < LBC_OUT; ++o) {
+        const float wo = wout ? wout[o] : 1.0f;
+        dy[o] = 2.0f * scale * wo * (Y[(uint64_t)r * LBC_OUT + o] - T[(uint64_t)r * LBC_OUT + o]);
+        DY[(uint64_t)r * LBC_OUT + o] = dy[o];
+    }
+    float d2[LBC_HID];
+#pragma unroll
+    for (int j = 0; j < LBC_HID; ++j) {
+        float s = 0.f;
+#pragma unroll
+        for (int o = 0; o < LBC_OUT; ++o) s += dy[o] * w[LBC_W3 + j * LBC_OUT + o];
+        d2[j] = s * gelu_d(A2[(uint64_t)r * LBC_HID + j]);
+        D2[(uint64_t)r * LBC_HID + j] = d2[j];
+    }
+    for (int i = 0; i < LBC_HID; ++i) {
+        float s = 0.f;
+#pragma unroll
+        for (int j = 0; j < LBC_HID; ++j) s += d2[j] * w[LBC_W2 + i * LBC_HID + j];
+        D1[(uint64_t)r * LBC_HID + i] = s * gelu_d(A1[(uint64_t)r * LBC_HID + i]);
+    }
+}
+
+// ---- training: weight gradients dW[k][n] = sum_r In[r][k] D[r][n], bias row k = K ------------
+// Block b sums rows b*rpb .. (b+1)*rpb - 1 into partial[b][(K + 1) * N]; the fold kernel then
+// adds the partials in block order (same partition, same order: deterministic).
+__global__ void __launch_bounds__(WG_THREADS) k_mlp_wgrad(const float *In, const float *D, int B, int K, int N,
+                                                          int rpb, float *partial)
+{
+    extern __shared__ float sh[];
+    float *si = sh;                       // [WG_ROWS][K]
+    float *sd = sh + WG_ROWS * K;         // [WG_ROWS][N]
+    const int KN = (K + 1) * N;
+    const int r0 = blockIdx.x * rpb, r1 = min(B, r0 + rpb);
+    float acc[28];
+#pragma unroll
+    for (int q = 0; q < 28; ++q) acc[q] = 0.f;
+    for (int rb = r0; rb < r1; rb += WG_ROWS) {
+        const int nr = min(WG_ROWS, r1 - rb);
+        __syncthreads();
+        for (int i = threadIdx.x; i < WG_ROWS * K; i += WG_THREADS) {
+            const int rr = i / K;
+            si[i] = rr < nr ? In[(uint64_t)(rb + rr) * K + (i - rr * K)] : 0.f;
+        }
+        for (int i = threadIdx.x; i < WG_ROWS * N; i += WG_THREADS) {
+            const int rr = i / N;
+            sd[i] = rr < nr ? D[(uint64_t)(rb + rr) * N + (i - rr * N)] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 28; ++q) {
+            const int e = threadIdx.x + q * WG_THREADS;
+            if (e >= KN) break;
+            const int k = e / N, n = e - k * N;
+            float s = acc[q];
+            if (k < K) {
+                for (int rr = 0; rr < WG_ROWS; ++rr) s += si[rr * K + k] * sd[rr * N + n];
+            } else {
+                for (int rr = 0; rr < WG_ROWS; ++rr) s += sd[rr * N + n];
+            }
+            acc[q] = s;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 28; ++q) {
+        const int e = threadIdx.x + q * WG_THREADS;
+        if (e < KN) partial[(uint64_t)blockIdx.x * KN + e] = acc[q];
+    }
+}
+
+// grad[w_off + k*N + n] (k < K) and grad[b_off + n] (bias) from the partials, blocks in order
+__global__ void k_mlp_wgrad_fold(const float *partial, int G, int K, int N, float *grad, int w_off, int b_off)
+{
+    const int KN = (K + 1) * N;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= KN) return;
+    float s = 0.f;
+    for (int b = 0; b < G; ++b) s += partial[(uint64_t)b * KN + e];
+    const int k = e / N, n = e - k * N;
+    if (k < K) grad[w_off + k * N + n] = s;
+    else grad[b_off + n] = s;
+}
+
+// ---- Adam (Kingma & Ba 2015) with bias correction ---------------------------------------------
+__global__ void k_adam(float *P, const float *G, float *M, float *V, int n, float lr, float b1, float b2,
+                       float eps, float c1, float c2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float g = G[i];
+    const float m = b1 * M[i] + (1.f - b1) * g;
+    const float v = b2 * V[i] + (1.f - b2) * g * g;
+    M[i] = m;
+    V[i] = v;
+    P[i] -= lr * (m / c1) / (sqrtf(v / c2) + eps);
+}
+
+// ---- inference ---------------------------------------------------------------------------------
+// A boundary step: every face's columns predict their ghosts from E^n, H^{n+1/2}
+// (r * MLP(stencil / r)): H^{n+1/2} outside side-0 faces, E^{n+1} outside side-1 faces; the E
+// update; the E fix-up; sources; the H update; the H fix-up (k_lbc_fix).
+constexpr int T_APPLY = 128;
+
+// float32 weights [6 faces][LBC_NPARAM] on the CUDA cores (the checker of the bfloat16 kernel)
+__global__ void __launch_bounds__(T_APPLY) k_lbc_predict32(const LGrid g, int side, const float *W,
+                                                           const float *E, const float *H, float *pred)
+{
+    __shared__ float w[LBC_NPARAM];
+    // blockIdx.y: face; its columns: blockIdx.x * T_APPLY + threadIdx.x
+    const int fi = blockIdx.y;
+    const LFace &f = g.face[fi];
+    if (side >= 0 && f.side != side) return;                 // block-uniform
+    const float *Wf = W + (uint64_t)(f.axis * 2 + f.side) * LBC_NPARAM;
+    for (int i = threadIdx.x; i < LBC_NPARAM; i += blockDim.x) w[i] = Wf[i];
+    __syncthreads();
+    const uint32_t c = blockIdx.x * T_APPLY + threadIdx.x;
+    if (c >= f.ncol) return;
+    const uint32_t u = f.u0 + c / f.nv, v = f.v0 + c % f.nv;
+    float *out = pred + (uint64_t)(f.col0 + c) * LBC_OUT;
+    // layer 1 is linear in the inputs: accumulate W1^T x on the raw stencil while summing its
+    // squares, then scale by 1/r (the normalisation) and add the bias
+    float a[LBC_HID], h[LBC_HID];
+#pragma unroll
+    for (int j = 0; j < LBC_HID; ++j) a[j] = 0.f;
+    float ss = 0.f;
+#pragma unroll
+    for (int d = 0; d < 2; ++d)
+#pragma unroll
+        for (int du = -1; du <= 1; ++du)
+#pragma unroll
+            for (int dv = -1; dv <= 1; ++dv) {
+                const uint64_t i = cell_of(g, f, u, v, d, du, dv);
+                const int k0 = ((d * 3 + (du + 1)) * 3 + (dv + 1)) * 6;
+#pragma unroll
+                for (int q = 0; q < 6; ++q) {
+                    const float xv = q < 3 ? E[q * g.N + i] : H[(q - 3) * g.N + i];
+                    ss += xv * xv;
+#pragma unroll
+                    for (int j = 0; j < LBC_HID; ++j) a[j] += xv * w[LBC_W1 + (k0 + q) * LBC_HID + j];
+                }
+            }
+    const float r = sqrtf(ss * (1.0f / LBC_IN));
+    if (!(r > 0.f)) {
+#pragma unroll
+        for (int o = 0; o < LBC_OUT; ++o) out[o] = 0.f;
+        return;
+    }
+    const float inv = 1.0f / r;
+#pragma unroll
+    for (int j = 0; j < LBC_HID; ++j) a[j] = w[LBC_B1 + j] + a[j] * inv;
+#pragma unroll
+    for (int j = 0; j < LBC_HID; ++j) h[j] = gelu(a[j]);
+#pragma unroll
+    for (int j = 0; j < LBC_HID; ++j) a[j] = w[LBC_B2 + j];
+#pragma unroll
+    for (int k = 0; k < LBC_HID; ++k) {
+        const float hk = h[k];
+#pragma unroll
+        for (int j = 0; j < LBC_HID; ++j) a[j] += hk * w[LBC_W2 + k * LBC_HID + j];
+    }
+#pragma unroll
+    for (int j = 0; j < LBC_HID; ++j) h[j] = gelu(a[j]);
+#pragma unroll
+    for (int o = 0; o < LBC_OUT; ++o) {
+        float y = w[LBC_B3 + o];
+#pragma unroll
+        for (int k = 0; k < LBC_HID; ++k) y += h[k] * w[LBC_W3 + k * LBC_OUT + o];
+        out[o] = y * r;
+    }
+}
+
+// ---- bfloat16 tensor-core inference (mma.sync m16n8k16, float32 accumulation) ------------------
+// Weights are packed once per face into the B-fragment order of mma.m16n8k16 (PTX ISA, "Matrix
+// fragments for mma.m16n8k16"): for k-step ks and n-tile nt, lane (g = lane / 4, t = lane % 4)
+// holds B[16 ks + 2t + {0, 1}][8 nt + g] in word 0 and B[16 ks + 2t + 8 + {0, 1}][8 nt + g] in
+// word 1, the lower k in the low half. Layer 1's K = 108 is padded to 112 with zero rows,
+// layer 3's N = 6 to 8 with zero columns. Biases stay float32.
+constexpr int PK_W1 = 0;                          // [7][8][32][2] words
+constexpr int PK_W2 = PK_W1 + 7 * 8 * 64;         // [4][8][32][2]
+constexpr int PK_W3 = PK_W2 + 4 * 8 * 64;         // [4][1][32][2]
+constexpr int PK_B1 = PK_W3 + 4 * 64;             // float [64]
+constexpr int PK_B2 = PK_B1 + LBC_HID;            // float [64]
+constexpr int PK_B3 = PK_B2 + LBC_HID;            // float [8]
+static_assert(PK_B3 + 8 == LBC_PACK_WORDS, "packed layout size");
+
+constexpr int MMA_WARPS = 4;
+constexpr int MMA_TILES = 4;                      // 16-column tiles per warp per block
+constexpr int MMA_COLS = MMA_WARPS * MMA_TILES * 16;
+constexpr int XS = 120;                           // float row stride of a warp's stencil tile
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+{
+    const uint32_t l = __bfloat16_as_ushort(__float2bfloat16_rn(lo));
+    const uint32_t h = __bfloat16_as_ushort(__float2bfloat16_rn(hi));
+    return l | (h << 16);
+}
+
+// x = hi + lo with hi = bf16(x), lo = bf16(x - hi): about 16 significant bits in two bf16 parts
+__device__ __forceinline__ void split_bf16(float x0, float x1, uint32_t &hi, uint32_t &lo)
+{
+    const __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
+    hi = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+    lo = pack_bf16(x0 - __bfloat162float(h0), x1 - __bfloat162float(h1));
+}
+
+__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__global__ void k_lbc_pack(const float *P, uint32_t *out)
+{
+    const int face = blockIdx.y;
+    const float *w = P + (uint64_t)face * LBC_NPARAM;
+    uint32_t *o = out + (uint64_t)face * LBC_PACK_WORDS;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < LBC_PACK_WORDS; e += gridDim.x * blockDim.x) {
+        uint32_t word;
+        if (e >= PK_B1) {
+            const int j = e - PK_B1;
+            const float b = j < LBC_HID ? w[LBC_B1 + j] : j < 2 * LBC_HID ? w[LBC_B2 + j - LBC_HID]
+                                                         : (j - 2 * LBC_HID < LBC_OUT ? w[LBC_B3 + j - 2 * LBC_HID] : 0.f);
+            word = __float_as_uint(b);
+        } else {
+            int base, K, N, nt_count, off;
+            if (e < PK_W2) { off = e - PK_W1; base = LBC_W1; K = LBC_IN; N = LBC_HID; nt_count = 8; }
+            else if (e < PK_W3) { off = e - PK_W2; base = LBC_W2; K = LBC_HID; N = LBC_HID; nt_count = 8; }
+            else { off = e - PK_W3; base = LBC_W3; K = LBC_HID; N = LBC_OUT; nt_count = 1; }
+            const int reg = off & 1, lane = (off >> 1) & 31, nt = (off >> 6) % nt_count, ks = (off >> 6) / nt_count;
+            const int g = lane >> 2, t = lane & 3;
+            const int k = 16 * ks + 2 * t + 8 * reg, n = 8 * nt + g;
+            const float v0 = (k < K && n < N) ? w[base + k * N + n] : 0.f;
+            const float v1 = (k + 1 < K && n < N) ? w[base + (k + 1) * N + n] : 0.f;
+            word = pack_bf16(v0, v1);
+        }
+        o[e] = word;
+    }
+}
+
+// GELU of a layer's accumulators, re-cut into the A fragments of the next layer: n-tiles 2 ks and
+// 2 ks + 1 of a 16 x 64 output are the k-step ks A fragment (rows g / g + 8, cols 2t / 2t + 8).
+template <bool SPLIT>
+__device__ __forceinline__ void act_to_a(const float acc[8][4], uint32_t ah[4][4], uint32_t al[4][4])
+{
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks)
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const float *c = acc[2 * ks + half];
+            const float g0 = gelu(c[0]), g1 = gelu(c[1]), g2 = gelu(c[2]), g3 = gelu(c[3]);
+            if (SPLIT) {
+                split_bf16(g0, g1, ah[ks][2 * half], al[ks][2 * half]);
+                split_bf16(g2, g3, ah[ks][2 * half + 1], al[ks][2 * half + 1]);
+            } else {
+                ah[ks][2 * half] = pack_bf16(g0, g1);
+                ah[ks][2 * half + 1] = pack_bf16(g2, g3);
+            }
+        }
+}
+
+template <bool SPLIT>
+__global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid g, int side, const uint32_t *Wp,
+                                                                     const float *E, const float *H, float *pred)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    uint32_t *w = smem;                                                   // LBC_PACK_WORDS
+    float *xs_all = reinterpret_cast<float *>(smem + LBC_PACK_WORDS);     // [warps][16][XS]
+    float *r_all = xs_all + MMA_WARPS * 16 * XS;                          // [warps][16] RMS of each row
+    const LFace &f = g.face[blockIdx.y];
+    if (side >= 0 && f.side != side) return;                             // block-uniform
+    {
+        const uint4 *src = reinterpret_cast<const uint4 *>(Wp + (uint64_t)(f.axis * 2 + f.side) * LBC_PACK_WORDS);
+        uint4 *dst = reinterpret_cast<uint4 *>(w);
+        for (int i = threadIdx.x; i < LBC_PACK_WORDS / 4; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gq = lane >> 2, tq = lane & 3;
+    float *xs = xs_all + warp * 16 * XS;
+    float *rr = r_all + warp * 16;
+    const float *wb = reinterpret_cast<const float *>(w);
+    const uint2 *w1 = reinterpret_cast<const uint2 *>(w + PK_W1);
+    const uint2 *w2 = reinterpret_cast<const uint2 *>(w + PK_W2);
+    const uint2 *w3 = reinterpret_cast<const uint2 *>(w + PK_W3);
+    for (int tile = 0; tile < MMA_TILES; ++tile) {
+        const uint32_t cbase = blockIdx.x * MMA_COLS + (tile * MMA_WARPS + warp) * 16;
+        if (cbase >= f.ncol) break;                                       // warp-uniform
+        // gather: lane pair (row = lane / 2) reads depth (lane & 1) of its column's stencil
+        {
+            const int row = lane >> 1, d = lane & 1;
+            const uint32_t c = cbase + row;
+            const bool ok = c < f.ncol;
+            const uint32_t cc = ok ? c : cbase;
+            const uint32_t u = f.u0 + cc / f.nv, v = f.v0 + cc % f.nv;
+            float x[54];
+            float ss = 0.f;
+#pragma unroll
+            for (int du = -1; du <= 1; ++du)
+#pragma unroll
+                for (int dv = -1; dv <= 1; ++dv) {
+                    const uint64_t i = cell_of(g, f, u, v, d, du, dv);
+                    const int k0 = ((du + 1) * 3 + (dv + 1)) * 6;
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) {
+                        const float xv = ok ? (q < 3 ? E[q * g.N + i] : H[(q - 3) * g.N + i]) : 0.f;
+                        x[k0 + q] = xv;
+                        ss += xv * xv;
+                    }
+                }
+            ss += __shfl_xor_sync(0xffffffffu, ss, 1);
+            const float r = sqrtf(ss * (1.0f / LBC_IN));
+            const float inv = r > 0.f ? 1.0f / r : 0.f;
+            float *xr = xs + row * XS + d * 54;
+#pragma unroll
+            for (int k = 0; k < 54; ++k) xr[k] = x[k] * inv;
+            if (d == 1) {
+#pragma unroll
+                for (int k = 108 - 54; k < 112 - 54; ++k) xr[k] = 0.f;   // K padding 108..111
+            } else {
+                rr[row] = r;
+            }
+        }
+        __syncwarp();
+        // layer 1: [16 x 112] x [112 x 64]
+        float acc[8][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const float b0 = wb[PK_B1 + 8 * nt + 2 * tq], b1 = wb[PK_B1 + 8 * nt + 2 * tq + 1];
+            acc[nt][0] = b0; acc[nt][1] = b1; acc[nt][2] = b0; acc[nt][3] = b1;
+        }
+#pragma unroll
+        for (int ks = 0; ks < 7; ++ks) {
+            const float2 p0 = *reinterpret_cast<const float2 *>(xs + gq * XS + 16 * ks + 2 * tq);
+            const float2 p1 = *reinterpret_cast<const float2 *>(xs + (gq + 8) * XS + 16 * ks + 2 * tq);
+            const float2 p2 = *reinterpret_cast<const float2 *>(xs + gq * XS + 16 * ks + 8 + 2 * tq);
+            const float2 p3 = *reinterpret_cast<const float2 *>(xs + (gq + 8) * XS + 16 * ks + 8 + 2 * tq);
+            uint32_t ah[4], al[4];
+            if (SPLIT) {
+                split_bf16(p0.x, p0.y, ah[0], al[0]);
+                split_bf16(p1.x, p1.y, ah[1], al[1]);
+                split_bf16(p2.x, p2.y, ah[2], al[2]);
+                split_bf16(p3.x, p3.y, ah[3], al[3]);
+            } else {
+                ah[0] = pack_bf16(p0.x, p0.y);
+                ah[1] = pack_bf16(p1.x, p1.y);
+                ah[2] = pack_bf16(p2.x, p2.y);
+                ah[3] = pack_bf16(p3.x, p3.y);
+            }
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const uint2 b = w1[(ks * 8 + nt) * 32 + lane];
+                mma_bf16(acc[nt], ah, b.x, b.y);
+                if (SPLIT) mma_bf16(acc[nt], al, b.x, b.y);
+            }
+        }
+        uint32_t ah2[4][4], al2[4][4];
+        act_to_a<SPLIT>(acc, ah2, al2);
+        // layer 2: [16 x 64] x [64 x 64]
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const float b0 = wb[PK_B2 + 8 * nt + 2 * tq], b1 = wb[PK_B2 + 8 * nt + 2 * tq + 1];
+            acc[nt][0] = b0; acc[nt][1] = b1; acc[nt][2] = b0; acc[nt][3] = b1;
+        }
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks)
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const uint2 b = w2[(ks * 8 + nt) * 32 + lane];
+                mma_bf16(acc[nt], ah2[ks], b.x, b.y);
+                if (SPLIT) mma_bf16(acc[nt], al2[ks], b.x, b.y);
+            }
+        act_to_a<SPLIT>(acc, ah2, al2);
+        // layer 3: [16 x 64] x [64 x 8]
+        float y[4];
+        {
+            const float b0 = wb[PK_B3 + 2 * tq], b1 = wb[PK_B3 + 2 * tq + 1];
+            y[0] = b0; y[1] = b1; y[2] = b0; y[3] = b1;
+        }
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+            const uint2 b = w3[ks * 32 + lane];
+            mma_bf16(y, ah2[ks], b.x, b.y);
+            if (SPLIT) mma_bf16(y, al2[ks], b.x, b.y);
+        }
+        // rows gq and gq + 8, output components 2 tq and 2 tq + 1 (< 6)
+        if (tq < 3) {
+#pragma unroll
+            for (int hr = 0; hr < 2; ++hr) {
+                const int row = gq + 8 * hr;
+                const uint32_t c = cbase + row;
+                if (c < f.ncol) {
+                    const float r = rr[row];
+                    float *out = pred + (uint64_t)(f.col0 + c) * LBC_OUT + 2 * tq;
+                    out[0] = r > 0.f ? y[2 * hr] * r : 0.f;
+                    out[1] = r > 0.f ? y[2 * hr + 1] * r : 0.f;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+constexpr size_t MMA_SMEM = (size_t)LBC_PACK_WORDS * 4 + (size_t)MMA_WARPS * 16 * (XS + 1) * 4;
+
+// Levi-Civita sign of distinct (q, a, p): +1 for the cyclic orders of (0, 1, 2)
+__device__ __forceinline__ float lc(int q, int a) { return ((a - q + 3) % 3) == 1 ? 1.f : -1.f; }
+
+__device__ __forceinline__ int own_of(const LGrid &g, uint32_t col)
+{
+    int f = 0;
+    while (f + 1 < g.nface && col >= g.own[f + 1].col0) ++f;
+    return f;
+}
+
+// one thread per outer cell: every learned face through the cell adds its term, faces in order
+__global__ void k_lbc_fix(const LGrid g, int fields, const float *pred, float *E, float *H, const float *ce,
+                          const float *cm, float dt)
+{
+    const uint32_t col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= g.nown) return;
+    const LFace &o = g.own[own_of(g, col)];
+    const uint32_t k = col - o.col0;
+    uint32_t c[3];
+    {
+        const int a = o.axis, ua = a == 0 ? 1 : 0, va = a == 2 ? 1 : 2;
+        c[a] = o.side ? g.s[a] - 1u : 0u;
+        c[ua] = o.u0 + k / o.nv;
+        c[va] = o.v0 + k % o.nv;
+    }
+    const uint64_t st[3] = {(uint64_t)g.s[1] * g.s[2], g.s[2], 1};
+    const uint64_t i = c[0] * st[0] + c[1] * st[1] + c[2];
+    float dE[3] = {0.f, 0.f, 0.f}, dH[3] = {0.f, 0.f, 0.f};
+    for (int fi = 0; fi < g.nface; ++fi) {
+        const LFace &f = g.face[fi];
+        const int a = f.axis, ua = a == 0 ? 1 : 0, va = a == 2 ? 1 : 2;
+        if (c[a] != (f.side ? g.s[a] - 1u : 0u)) continue;
+        const float *gp = pred + ((uint64_t)f.col0 + (uint64_t)c[ua] * f.nv + c[va]) * LBC_OUT;
+        // the wrapped neighbour: index s_a - 1 (side 0) or 0 (side 1) along a
+        const uint64_t j = f.side ? i - (uint64_t)(g.s[a] - 1u) * st[a] : i + (uint64_t)(g.s[a] - 1u) * st[a];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            if (q == a) continue;
+            const int p = 3 - a - q;
+            if (f.side == 0 && (fields & LBC_FIX_E)) dE[q] -= lc(q, a) * (gp[3 + p] - H[p * g.N + j]);
+            if (f.side == 1 && (fields & LBC_FIX_H)) dH[q] -= lc(q, a) * (gp[p] - E[p * g.N + j]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        if ((fields & LBC_FIX_E) && dE[q] != 0.f) E[q * g.N + i] += ce[q * g.N + i] * dE[q];
+        if ((fields & LBC_FIX_H) && dH[q] != 0.f) H[q * g.N + i] += (cm ? cm[q * g.N + i] : dt) * dH[q];
+    }
+}
+
+}  // namespace
+
+// the column grids of the faces in face_mask (bit 2a + side): whole planes, and owned cells
+LGrid lbc_grid(const uint32_t s[3], int face_mask)
+{
+    LGrid g;
+    g.s[0] = s[0];
+    g.s[1] = s[1];
+    g.s[2] = s[2];
+    g.N = (uint64_t)s[0] * s[1] * s[2];
+    g.mask = face_mask;
+    g.nface = 0;
+    g.ncol = 0;
+    g.nown = 0;
+    bool owned[3][2] = {{false, false}, {false, false}, {false, false}};
+    for (int a = 0; a < 3; ++a)
+        for (int side = 0; side < 2; ++side) {
+            if (!(face_mask & (1 << (2 * a + side)))) continue;
+            const int ua = a == 0 ? 1 : 0, va = a == 2 ? 1 : 2;
+            LFace f;
+            f.axis = a;
+            f.side = side;
+            f.u0 = 0;
+            f.v0 = 0;
+            f.nu = s[ua];
+            f.nv = s[va];
+            f.ncol = f.nu * f.nv;
+            f.col0 = g.ncol;
+            g.ncol += f.ncol;
+            // owned: skip the cells of an earlier face's plane (lower axes own the edges)
+            LFace o = f;
+            uint32_t u0 = 0, u1 = s[ua], v0 = 0, v1 = s[va];
+            if (owned[ua][0]) u0 = 1;
+            if (owned[ua][1] && u1 > 0) u1 -= 1;
+            if (owned[va][0]) v0 = 1;
+            if (owned[va][1] && v1 > 0) v1 -= 1;
+            o.u0 = u0;
+            o.v0 = v0;
+            o.nu = u1 > u0 ? u1 - u0 : 0;
+            o.nv = v1 > v0 ? v1 - v0 : 0;
+            o.ncol = o.nu * o.nv;
+            o.col0 = g.nown;
+            g.nown += o.ncol;
+            g.face[g.nface] = f;
+            g.own[g.nface] = o;
+            ++g.nface;
+            owned[a][side] = true;
+        }
+    return g;
+}
+
+cudaError_t launch_lbc_gather(const LGrid &g, const float *E, const float *H, float *X, float *R, float *C,
+                              cudaStream_t st)
+{
+    if (!g.ncol) return cudaSuccess;
+    k_lbc_gather<<<(g.ncol + 127) / 128, 128, 0, st>>>(g, E, H, X, R, C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_fwd(const float *P, const float *X, int B, float *Y, float *A1, float *A2, float *H1,
+                           float *H2, cudaStream_t st)
+{
+    if (B <= 0) return cudaSuccess;
+    k_mlp_fwd<<<(B + T_FWD - 1) / T_FWD, T_FWD, 0, st>>>(P, X, B, Y, A1, A2, H1, H2);
+    return cudaGetLastError();
+}
+
+// workspace floats needed by launch_mlp_bwd for a batch of B
+size_t mlp_bwd_workspace(int B)
+{
+    const int G = (B + 255) / 256;
+    return (size_t)B * (LBC_OUT + 2 * LBC_HID) + (size_t)G * (LBC_IN + 1) * LBC_HID;
+}
+
+cudaError_t launch_mlp_bwd(const float *P, const float *X, const float *Y, const float *T, const float *wout,
+                           int B, const float *A1, const float *A2, const float *H1, const float *H2,
+                           float *grad, float *ws, cudaStream_t st)
+{
+    if (B <= 0) return cudaSuccess;
+    float *DY = ws, *D2 = DY + (size_t)B * LBC_OUT, *D1 = D2 + (size_t)B * LBC_HID;
+    float *part = D1 + (size_t)B * LBC_HID;
+    k_mlp_bwd_rows<<<(B + T_FWD - 1) / T_FWD, T_FWD, 0, st>>>(P, Y, T, wout, B, 1.0f / ((float)B * LBC_OUT),
+                                                              A1, A2, DY, D2, D1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int rpb = 256, G = (B + rpb - 1) / rpb;
+    struct L { const float *in; const float *d; int K, N, w, b; } layers[3] = {
+        {X, D1, LBC_IN, LBC_HID, LBC_W1, LBC_B1},
+        {H1, D2, LBC_HID, LBC_HID, LBC_W2, LBC_B2},
+        {H2, DY, LBC_HID, LBC_OUT, LBC_W3, LBC_B3}};
+    for (const L &l : layers) {
+        const size_t smem = (size_t)WG_ROWS * (l.K + l.N) * sizeof(float);
+        k_mlp_wgrad<<<G, WG_THREADS, smem, st>>>(l.in, l.d, B, l.K, l.N, rpb, part);
+        const int KN = (l.K + 1) * l.N;
+        k_mlp_wgrad_fold<<<(KN + 255) / 256, 256, 0, st>>>(part, G, l.K, l.N, grad, l.w, l.b);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// out[(K + 1) x N]: A^T B (rows k < K) and the column sums of B (row K), A [rows][K], B [rows][N]
+// (K, N with (K + 1) N <= 28 * WG_THREADS); ws: ceil(rows / 256) * (K + 1) * N floats
+size_t gram_workspace(int rows, int K, int N) { return (size_t)((rows + 255) / 256) * (K + 1) * N; }
+
+cudaError_t launch_gram(const float *A, int rows, int K, const float *B, int N, float *out, float *ws,
+                        cudaStream_t st)
+{
+    if (rows <= 0) return cudaSuccess;
+    const int rpb = 256, G = (rows + rpb - 1) / rpb;
+    const size_t smem = (size_t)WG_ROWS * (K + N) * sizeof(float);
+    k_mlp_wgrad<<<G, WG_THREADS, smem, st>>>(A, B, rows, K, N, rpb, ws);
+    const int KN = (K + 1) * N;
+    k_mlp_wgrad_fold<<<(KN + 255) / 256, 256, 0, st>>>(ws, G, K, N, out, 0, K * N);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adam(float *P, const float *G, float *M, float *V, int n, float lr, float b1, float b2,
+                        float eps, int step, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+    k_adam<<<(n + 255) / 256, 256, 0, st>>>(P, G, M, V, n, lr, b1, b2, eps, c1, c2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lbc_pack(const float *P, uint32_t *out, cudaStream_t st)
+{
+    k_lbc_pack<<<dim3((LBC_PACK_WORDS + 255) / 256, 6, 1), 256, 0, st>>>(P, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lbc_predict(const LGrid &g, int side, int precision, const void *W, const float *E,
+                               const float *H, float *pred, cudaStream_t st)
+{
+    if (!g.ncol) return cudaSuccess;
+    uint32_t maxc = 0;
+    for (int f = 0; f < g.nface; ++f) maxc = g.face[f].ncol > maxc ? g.face[f].ncol : maxc;
+    if (precision == LBC_F32) {
+        const dim3 gi((maxc + T_APPLY - 1) / T_APPLY, (unsigned)g.nface, 1);
+        k_lbc_predict32<<<gi, T_APPLY, 0, st>>>(g, side, (const float *)W, E, H, pred);
+        return cudaGetLastError();
+    }
+    static bool attr_set[2] = {false, false};
+    const int split = precision == LBC_BF16X2 ? 1 : 0;
+    cudaError_t e;
+    if (!attr_set[split]) {
+        e = split ? cudaFuncSetAttribute(k_lbc_predict_mma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MMA_SMEM)
+                  : cudaFuncSetAttribute(k_lbc_predict_mma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MMA_SMEM);
+        if (e != cudaSuccess) return e;
+        attr_set[split] = true;
+    }
+    const dim3 gi((maxc + MMA_COLS - 1) / MMA_COLS, (unsigned)g.nface, 1);
+    if (split) k_lbc_predict_mma<true><<<gi, MMA_WARPS * 32, MMA_SMEM, st>>>(g, side, (const uint32_t *)W, E, H, pred);
+    else k_lbc_predict_mma<false><<<gi, MMA_WARPS * 32, MMA_SMEM, st>>>(g, side, (const uint32_t *)W, E, H, pred);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lbc_fix(const LGrid &g, int fields, const float *pred, float *E, float *H, const float *ce,
+                           const float *cm, float dt, cudaStream_t st)
+{
+    if (!g.nown) return cudaSuccess;
+    k_lbc_fix<<<(g.nown + 127) / 128, 128, 0, st>>>(g, fields, pred, E, H, ce, cm, dt);
+    return cudaGetLastError();
+}
+
+}  // namespace fdtd
