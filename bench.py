@@ -696,35 +696,55 @@ def run_c4(args):
 
 
 def run_c5(args):
-    """Learned thin boundary on the c2 cavity: train the boundary network (teacher runs, ridge
-    least-squares start, Adam fine-tune, all on the device), judge it (reflection against a
-    doubled grid, long-run stability), then time the c2 cavity (a) plain with its 8-cell CPML
-    (395x345x73) and (b) cut to its useful interior plus a 2-cell learned layer per face
-    (383x333x61), and report the form the judge deploys. Throughput counts useful-interior
-    cells (379x329x57 in both forms)."""
+    """Learned thin boundary on the c2 cavity: teacher data (Mur-memory targets), candidate
+    networks (least squares shrunk towards Mur's map at two strengths, and Mur's map itself),
+    the judge on each (reflection against a doubled grid, long-run stability), then the c2
+    cavity timed (a) plain with its 8-cell CPML (395x345x73) and (b) cut to its useful
+    interior plus a 2-cell learned layer per face (383x333x61) with the picked candidate; the
+    line reports the form the judge deploys. Throughput counts useful-interior cells
+    (379x329x57 in both forms)."""
     import torch
     from opencl_fdtd_gb300 import Simulation, workloads
     from opencl_fdtd_gb300 import learned_boundary as L
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
-    net, data, start, fin = L.train(runs=args.c5_runs, seed=5)
+    data = L.make_teacher_data(runs=args.c5_runs, seed=5, memory=L.MUR_MEMORY)
+    torch.cuda.synchronize()
+    data_s = time.perf_counter() - t0
+    probe = L.BoundaryNet(seed=6, memory=L.MUR_MEMORY)
+    tvar = {f: float(((data.T[f] ** 2) * probe.output_weights(f)).mean()) for f in range(6)}
+    samples = data.sizes()
+    # candidates: least squares shrunk towards Mur's map (two strengths), and Mur's map itself;
+    # the judge (bf16x2 inference, the deployed precision) picks the best accepted one
+    cands = {}
+    t0 = time.perf_counter()
+    for name, rho in (("learned, shrink 0.3", 0.3), ("learned, shrink 1", 1.0), ("Mur first order", None)):
+        net_c = L.BoundaryNet(seed=6, memory=L.MUR_MEMORY)
+        if rho is None:
+            for f in range(6):
+                net_c.embed_linear(f, L.mur_map(f))
+        else:
+            net_c.fit_linear(data, ridge=rho, prior="mur")
+        rel_c = [round(net_c.loss(f, data.X[f], data.T[f]) / tvar[f], 5) for f in range(6)]
+        cands[name] = (net_c, rel_c)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
-    tvar = {f: float(((data.T[f] ** 2) * net.output_weights(f)).mean()) for f in range(6)}
-    rel = {"start": [round(start[f] / tvar[f], 5) for f in range(6)],
-           "finetuned": [round(fin[f] / tvar[f], 5) for f in range(6)]}
-    samples = data.sizes()
     del data
     torch.cuda.empty_cache()
-    lb = L.LearnedBoundary(net, "bf16")
     t0 = time.perf_counter()
-    verdict = L.judge(lb)
+    verdicts = {name: L.judge(L.LearnedBoundary(n_, "bf16x2")) for name, (n_, _) in cands.items()}
     judge_s = time.perf_counter() - t0
-    zero = L.BoundaryNet(seed=3)
+    accepted = [k for k, v in verdicts.items() if v["accepted"]]
+    pick = min(accepted, key=lambda k: verdicts[k]["reflection_db"]) if accepted else "learned, shrink 0.3"
+    net = cands[pick][0]
+    verdict = verdicts[pick]
+    lb = L.LearnedBoundary(net, "bf16x2")
+    zero = L.BoundaryNet(seed=3, memory=L.MUR_MEMORY)
     zero.params.zero_()
-    held = L.reflection_db(L.LearnedBoundary(zero, "bf16"), shape=(96, 96, 96), steps=400, period=20.0)
+    held = L.reflection_db(L.LearnedBoundary(zero, "bf16x2"), shape=(96, 96, 96), steps=400, period=20.0)
     first_pass = L.reflection_db(lb, shape=(96, 96, 96), steps=250, period=20.0)
-    held_first = L.reflection_db(L.LearnedBoundary(zero, "bf16"), shape=(96, 96, 96), steps=250, period=20.0)
+    held_first = L.reflection_db(L.LearnedBoundary(zero, "bf16x2"), shape=(96, 96, 96), steps=250, period=20.0)
+    rel = {name: r for name, (_, r) in cands.items()}
 
     # the c2 cavity: plain with its CPML, and cut to the useful interior plus the 2-cell layer
     K = args.c5_steps
@@ -777,12 +797,13 @@ def run_c5(args):
     l2 = float(torch.linalg.norm((Et - Ep).double()) / torch.linalg.norm(Ep.double())) if finite else float("inf")
     # the network's share of a thin step: one predict launch per step, timed alone
     n_cols, _ = L.columns(thin_shape)
-    W = net.weights("bf16")
+    W = net.weights("bf16x2")
     pred = torch.empty(n_cols * 6, dtype=torch.float32, device="cuda")
     lib = L._lib.load()
 
     def predict():
-        L._lib.check(lib.fdtd_lbc_predict(L._shape_arg(thin_shape), 63, -1, L.PRECISIONS["bf16"], W.data_ptr(),
+        L._lib.check(lib.fdtd_lbc_predict(L._shape_arg(thin_shape), 63, -1, L.PRECISIONS["bf16x2"], net.memory,
+                                          W.data_ptr(),
                                           thin.E.data_ptr(), thin.H.data_ptr(), pred.data_ptr(), pred.numel(),
                                           ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
     thin.E.zero_()
@@ -816,7 +837,8 @@ def run_c5(args):
         "metric": METRIC + " (useful interior)", "value": round(value, 2), "unit": UNIT, "n_gpus": 1, "steps": K,
         "warmup": 3, "ms_per_step": round((ms_thin if deployed == "learned" else ms_plain) / K, 5),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 fields; boundary MLP bf16 weights, f32 accumulation", "data": "synthetic (seeded)",
+        "dtype": "f32 fields; boundary MLP bf16 weights, f32 accumulation (bf16x2 activations)",
+        "data": "synthetic (seeded)",
         "config": {"workload": "c5: c2 cavity %s, useful interior %s; 2-cell learned layer (%s grid) or "
                                "8-cell CPML; Poynting on; %d steps" % ("x".join(map(str, shape)),
                                                                       "x".join(map(str, useful)),
@@ -824,14 +846,16 @@ def run_c5(args):
                    "teacher": "%d runs at 128^3, 16-cell CPML, 1500 steps, 1-8 spheres eps U[1,12] inside "
                               "the box, dipole pulse period U[10,30] steps, random polarisation" % args.c5_runs,
                    "l2": "c2 fields (%.0f MB) larger than the 129 MB L2; no flush" % (int(numpy.prod(shape)) * 36 / 1e6)},
-        "deployed": deployed,
-        "verdict": {k: (round(v, 2) if isinstance(v, float) and math.isfinite(v) else v) for k, v in verdict.items()
-                    if k != "reflection_by_period"},
-        "reflection_by_period_db": {str(k): round(v, 2) for k, v in verdict["reflection_by_period"].items()},
+        "deployed": deployed, "candidate_timed": pick,
+        "verdicts": {name: {k: (round(v, 2) if isinstance(v, float) and math.isfinite(v) else
+                                ({str(a): round(b, 2) for a, b in v.items()} if isinstance(v, dict) else v))
+                            for k, v in vd.items()} for name, vd in verdicts.items()},
         "first_pass_reflection_db": {"learned": round(first_pass["reflection_db"], 2),
                                      "zero_ghost_layer": round(held_first["reflection_db"], 2)},
         "zero_ghost_layer_reflection_db": round(held["reflection_db"], 2),
-        "training": {"seconds": round(train_s, 1), "samples_per_face": samples, "relative_loss": rel},
+        "training": {"data_seconds": round(data_s, 1), "fit_seconds": round(train_s, 1),
+                     "samples_per_face": samples, "memory": round(L.MUR_MEMORY, 5),
+                     "relative_loss_per_face": rel},
         "judge_seconds": round(judge_s, 1),
         "plain_cpml8": {"ms": round(ms_plain, 3), "useful_mcells_per_s": round(v_plain, 2),
                         "grid": list(shape)},
@@ -841,7 +865,8 @@ def run_c5(args):
                          "predict_ms_per_step": round(ms_pred, 4), "boundary_columns": n_cols},
         "roofline": {"bound": "tensor", "achieved": round(flops / (ms_pred * 1e-3) / 1e12, 2),
                      "peak": tc_peak, "unit": "TFLOP/s", "frac": round(flops / (ms_pred * 1e-3) / 1e12 / tc_peak, 4),
-                     "traffic": None, "kernel": "k_lbc_predict_mma (bf16 mma.sync)"},
+                     "traffic": None, "kernel": "k_lbc_predict_mma<split> (bf16 mma.sync, algorithmic FLOPs "
+                                               "of one bf16 pass)"},
         "gpu_launches": "thin: 4 + the plain step's per step; plain: the plain step's",
     }
     print(json.dumps(line), flush=True)

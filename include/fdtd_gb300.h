@@ -347,9 +347,12 @@ int fdtd_adam(float *params, const float *grad, float *m, float *v, int32_t n, f
               float beta2, float eps, int32_t step, void *stream);
 /* float32 parameters [6][LBC_NPARAM] -> bfloat16 tensor-core layout [6][LBC_PACK_WORDS]. */
 int fdtd_lbc_pack(const float *params, void *packed, void *stream);
-/* Ghost values [ncol][6] (r times the network output) of the faces of side `side` (-1: all);
- * weights: float32 parameters (FDTD_LBC_F32) or the packed layout (BF16, BF16X2). */
-int fdtd_lbc_predict(const int32_t shape[3], int32_t face_mask, int32_t side, int32_t precision,
+/* Ghost values [ncol][6] of the faces of side `side` (-1: all): pred = r * (network output)
+ * + memory * pred, pred holding the previous step's ghosts (zero before the first step);
+ * weights: float32 parameters (FDTD_LBC_F32) or the packed layout (BF16, BF16X2). memory =
+ * (1 - c dt) / (1 + c dt) makes room for Mur's first-order condition (its other terms are
+ * linear in the stencil); memory = 0: ghosts from the current stencil alone. */
+int fdtd_lbc_predict(const int32_t shape[3], int32_t face_mask, int32_t side, int32_t precision, float memory,
                      const void *weights, const float *E, const float *H, float *pred, int64_t pred_floats,
                      void *stream);
 /* Replace, in the updates of the outermost cells, the wrapped neighbour by the ghost:
@@ -365,8 +368,8 @@ int fdtd_lbc_fix(const int32_t shape[3], int32_t face_mask, int32_t fields, cons
 /* Make fdtd_run step the plan with the learned boundary (float32 plans with unit cells and no
  * Bloch boundaries; face_mask 0 detaches). weights and pred (ncol x 6 floats) stay owned by
  * the caller and must outlive the attachment. The faces in face_mask should carry no CPML. */
-int fdtd_lbc_attach(FdtdPlan *plan, int32_t face_mask, int32_t precision, const void *weights, float *pred,
-                    int64_t pred_floats);
+int fdtd_lbc_attach(FdtdPlan *plan, int32_t face_mask, int32_t precision, float memory, const void *weights,
+                    float *pred, int64_t pred_floats);
 
 #ifdef __cplusplus
 }

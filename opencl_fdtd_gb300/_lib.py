@@ -133,9 +133,10 @@ SIGNATURES = [
     ("fdtd_adam", c_i32, [c_vp, c_vp, c_vp, c_vp, c_i32, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                           ctypes.c_float, c_i32, c_vp]),
     ("fdtd_lbc_pack", c_i32, [c_vp, c_vp, c_vp]),
-    ("fdtd_lbc_predict", c_i32, [_P(c_i32), c_i32, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    ("fdtd_lbc_predict", c_i32, [_P(c_i32), c_i32, c_i32, c_i32, ctypes.c_float, c_vp, c_vp, c_vp, c_vp, c_i64,
+                                 c_vp]),
     ("fdtd_lbc_fix", c_i32, [_P(c_i32), c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_f64, c_vp]),
-    ("fdtd_lbc_attach", c_i32, [c_vp, c_i32, c_i32, c_vp, c_vp, c_i64]),
+    ("fdtd_lbc_attach", c_i32, [c_vp, c_i32, c_i32, ctypes.c_float, c_vp, c_vp, c_i64]),
 ]
 
 FDTD_LBC_IN = 108

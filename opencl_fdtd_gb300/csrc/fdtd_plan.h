@@ -26,6 +26,7 @@ struct FdtdPlan {
     // learned boundary attached with fdtd_lbc_attach (lbc_mask 0: none)
     int32_t lbc_mask = 0;       // faces, bit 2 * axis + side
     int32_t lbc_precision = 0;  // FDTD_LBC_F32 / BF16 / BF16X2
+    float lbc_memory = 0.f;     // weight of the previous step's ghosts
     const void *lbc_w = nullptr;
     float *lbc_pred = nullptr;  // [columns][6] predictions of the current step
 };

@@ -257,13 +257,15 @@ __global__ void k_adam(float *P, const float *G, float *M, float *V, int n, floa
 }
 
 // ---- inference ---------------------------------------------------------------------------------
-// A boundary step: every face's columns predict their ghosts from E^n, H^{n+1/2}
-// (r * MLP(stencil / r)): H^{n+1/2} outside side-0 faces, E^{n+1} outside side-1 faces; the E
-// update; the E fix-up; sources; the H update; the H fix-up (k_lbc_fix).
+// A boundary step: every face's columns predict their ghosts from E^n, H^{n+1/2}, as
+// r * MLP(stencil / r) + memory * (the previous step's ghost): H^{n+1/2} outside side-0 faces,
+// E^{n+1} outside side-1 faces; the E update; the E fix-up; sources; the H update; the H fix-up
+// (k_lbc_fix). With memory = (1 - c dt) / (1 + c dt) the form contains Mur's first-order
+// absorbing condition written for the ghost (the rest of Mur's update is linear in the stencil).
 constexpr int T_APPLY = 128;
 
 // float32 weights [6 faces][LBC_NPARAM] on the CUDA cores (the checker of the bfloat16 kernel)
-__global__ void __launch_bounds__(T_APPLY) k_lbc_predict32(const LGrid g, int side, const float *W,
+__global__ void __launch_bounds__(T_APPLY) k_lbc_predict32(const LGrid g, int side, float memory, const float *W,
                                                            const float *E, const float *H, float *pred)
 {
     __shared__ float w[LBC_NPARAM];
@@ -303,7 +305,7 @@ __global__ void __launch_bounds__(T_APPLY) k_lbc_predict32(const LGrid g, int si
     const float r = sqrtf(ss * (1.0f / LBC_IN));
     if (!(r > 0.f)) {
 #pragma unroll
-        for (int o = 0; o < LBC_OUT; ++o) out[o] = 0.f;
+        for (int o = 0; o < LBC_OUT; ++o) out[o] = memory * out[o];
         return;
     }
     const float inv = 1.0f / r;
@@ -326,7 +328,7 @@ __global__ void __launch_bounds__(T_APPLY) k_lbc_predict32(const LGrid g, int si
         float y = w[LBC_B3 + o];
 #pragma unroll
         for (int k = 0; k < LBC_HID; ++k) y += h[k] * w[LBC_W3 + k * LBC_OUT + o];
-        out[o] = y * r;
+        out[o] = y * r + memory * out[o];
     }
 }
 
@@ -423,8 +425,9 @@ __device__ __forceinline__ void act_to_a(const float acc[8][4], uint32_t ah[4][4
 }
 
 template <bool SPLIT>
-__global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid g, int side, const uint32_t *Wp,
-                                                                     const float *E, const float *H, float *pred)
+__global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid g, int side, float memory,
+                                                                     const uint32_t *Wp, const float *E,
+                                                                     const float *H, float *pred)
 {
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t *w = smem;                                                   // LBC_PACK_WORDS
@@ -555,8 +558,8 @@ __global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid 
                 if (c < f.ncol) {
                     const float r = rr[row];
                     float *out = pred + (uint64_t)(f.col0 + c) * LBC_OUT + 2 * tq;
-                    out[0] = r > 0.f ? y[2 * hr] * r : 0.f;
-                    out[1] = r > 0.f ? y[2 * hr + 1] * r : 0.f;
+                    out[0] = (r > 0.f ? y[2 * hr] * r : 0.f) + memory * out[0];
+                    out[1] = (r > 0.f ? y[2 * hr + 1] * r : 0.f) + memory * out[1];
                 }
             }
         }
@@ -747,7 +750,7 @@ cudaError_t launch_lbc_pack(const float *P, uint32_t *out, cudaStream_t st)
     return cudaGetLastError();
 }
 
-cudaError_t launch_lbc_predict(const LGrid &g, int side, int precision, const void *W, const float *E,
+cudaError_t launch_lbc_predict(const LGrid &g, int side, int precision, float memory, const void *W, const float *E,
                                const float *H, float *pred, cudaStream_t st)
 {
     if (!g.ncol) return cudaSuccess;
@@ -755,7 +758,7 @@ cudaError_t launch_lbc_predict(const LGrid &g, int side, int precision, const vo
     for (int f = 0; f < g.nface; ++f) maxc = g.face[f].ncol > maxc ? g.face[f].ncol : maxc;
     if (precision == LBC_F32) {
         const dim3 gi((maxc + T_APPLY - 1) / T_APPLY, (unsigned)g.nface, 1);
-        k_lbc_predict32<<<gi, T_APPLY, 0, st>>>(g, side, (const float *)W, E, H, pred);
+        k_lbc_predict32<<<gi, T_APPLY, 0, st>>>(g, side, memory, (const float *)W, E, H, pred);
         return cudaGetLastError();
     }
     static bool attr_set[2] = {false, false};
@@ -768,8 +771,10 @@ cudaError_t launch_lbc_predict(const LGrid &g, int side, int precision, const vo
         attr_set[split] = true;
     }
     const dim3 gi((maxc + MMA_COLS - 1) / MMA_COLS, (unsigned)g.nface, 1);
-    if (split) k_lbc_predict_mma<true><<<gi, MMA_WARPS * 32, MMA_SMEM, st>>>(g, side, (const uint32_t *)W, E, H, pred);
-    else k_lbc_predict_mma<false><<<gi, MMA_WARPS * 32, MMA_SMEM, st>>>(g, side, (const uint32_t *)W, E, H, pred);
+    if (split)
+        k_lbc_predict_mma<true><<<gi, MMA_WARPS * 32, MMA_SMEM, st>>>(g, side, memory, (const uint32_t *)W, E, H, pred);
+    else
+        k_lbc_predict_mma<false><<<gi, MMA_WARPS * 32, MMA_SMEM, st>>>(g, side, memory, (const uint32_t *)W, E, H, pred);
     return cudaGetLastError();
 }
 

@@ -70,10 +70,10 @@ cudaError_t launch_adam(float *P, const float *G, float *M, float *V, int n, flo
                         float eps, int step, cudaStream_t st);
 // float32 parameters [6 faces][LBC_NPARAM] -> packed [6][LBC_PACK_WORDS]
 cudaError_t launch_lbc_pack(const float *P, uint32_t *out, cudaStream_t st);
-// ghost values [ncol][6] of the faces of side `side` (-1: all faces); W: float32 parameters
-// [6][LBC_NPARAM] (LBC_F32) or packed words [6][LBC_PACK_WORDS] (LBC_BF16, LBC_BF16X2),
-// face = 2 * axis + side
-cudaError_t launch_lbc_predict(const LGrid &g, int side, int precision, const void *W, const float *E,
+// ghost values [ncol][6] of the faces of side `side` (-1: all faces): pred = r * net + memory *
+// pred (the previous ghosts); W: float32 parameters [6][LBC_NPARAM] (LBC_F32) or packed words
+// [6][LBC_PACK_WORDS] (LBC_BF16, LBC_BF16X2), face = 2 * axis + side
+cudaError_t launch_lbc_predict(const LGrid &g, int side, int precision, float memory, const void *W, const float *E,
                                const float *H, float *pred, cudaStream_t st);
 // The plain update of a grid whose edges wrap reads, across a learned side-0 face of axis a,
 // H_p at index s_a - 1 for E_q at index 0 (q, a, p distinct), and across a learned side-1 face

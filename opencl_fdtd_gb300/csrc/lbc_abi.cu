@@ -44,8 +44,9 @@ static LGrid plan_grid(const FdtdPlan *p)
 int lbc_before_e(const FdtdPlan *p, const FdtdBuffers *b, const void *H, cudaStream_t st)
 {
     if (!p->lbc_mask) return FDTD_OK;
-    return check_cuda(launch_lbc_predict(plan_grid(p), -1, p->lbc_precision, p->lbc_w, (const float *)b->E,
-                                         (const float *)H, p->lbc_pred, st), "lbc predict launch");
+    return check_cuda(launch_lbc_predict(plan_grid(p), -1, p->lbc_precision, p->lbc_memory, p->lbc_w,
+                                         (const float *)b->E, (const float *)H, p->lbc_pred, st),
+                      "lbc predict launch");
 }
 
 int lbc_after_e(const FdtdPlan *p, const FdtdBuffers *b, const void *H, cudaStream_t st)
@@ -164,7 +165,7 @@ static int check_weights(int32_t precision, const void *weights, const char *wha
     return FDTD_OK;
 }
 
-int fdtd_lbc_predict(const int32_t shape[3], int32_t face_mask, int32_t side, int32_t precision,
+int fdtd_lbc_predict(const int32_t shape[3], int32_t face_mask, int32_t side, int32_t precision, float memory,
                      const void *weights, const float *E, const float *H, float *pred, int64_t pred_floats,
                      void *stream)
 {
@@ -176,7 +177,7 @@ int fdtd_lbc_predict(const int32_t shape[3], int32_t face_mask, int32_t side, in
     if (side < -1 || side > 1) return bad("fdtd_lbc_predict: side must be -1, 0 or 1");
     const LGrid g = grid_of(shape, face_mask);
     if (pred_floats < (int64_t)g.ncol * LBC_OUT) return bad("fdtd_lbc_predict: pred too small");
-    return check_cuda(launch_lbc_predict(g, side, precision, weights, E, H, pred, (cudaStream_t)stream),
+    return check_cuda(launch_lbc_predict(g, side, precision, memory, weights, E, H, pred, (cudaStream_t)stream),
                       "lbc predict launch");
 }
 
@@ -193,8 +194,8 @@ int fdtd_lbc_fix(const int32_t shape[3], int32_t face_mask, int32_t fields, cons
                                      (cudaStream_t)stream), "lbc fix launch");
 }
 
-int fdtd_lbc_attach(FdtdPlan *plan, int32_t face_mask, int32_t precision, const void *weights, float *pred,
-                    int64_t pred_floats)
+int fdtd_lbc_attach(FdtdPlan *plan, int32_t face_mask, int32_t precision, float memory, const void *weights,
+                    float *pred, int64_t pred_floats)
 {
     if (!plan) return bad("fdtd_lbc_attach: plan is NULL");
     if (face_mask < 0 || face_mask > 63) return bad("fdtd_lbc_attach: face_mask must be in [0, 63]");
@@ -216,6 +217,7 @@ int fdtd_lbc_attach(FdtdPlan *plan, int32_t face_mask, int32_t precision, const 
     if (pred_floats < (int64_t)g.ncol * LBC_OUT) return bad("fdtd_lbc_attach: pred too small");
     plan->lbc_mask = face_mask;
     plan->lbc_precision = precision;
+    plan->lbc_memory = memory;
     plan->lbc_w = weights;
     plan->lbc_pred = pred;
     return FDTD_OK;

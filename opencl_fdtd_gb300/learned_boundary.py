@@ -38,12 +38,16 @@ faces relative to the largest field that reached that shell, and a long run chec
 error does not grow (the boundary feeds its own output back every step). A boundary that is
 worse than the threshold (-40 dB by default) or grows is replaced by CPML.
 
-Measured behaviour: the trained ghost map predicts the ghost fields to a few percent RMS and,
-over the first pass of a pulse, leaves an error tens of dB below the same 2-cell layer
-without the network (zero ghosts); in closed-loop feedback every map trained so far (MLP from
-a random start, ridge least squares, input noise, edge treatments) develops an error that grows
-by a few percent per step after some hundreds of steps, so the judge rejects it and the
-simulation falls back to CPML.
+Memory term: a ghost is predicted as r * MLP(x) + memory * (the previous step's ghost). With
+memory = (1 - c dt) / (1 + c dt) the form contains Mur's first-order absorbing condition
+(``mur_map``), and training can shrink the fitted map towards Mur's (``fit_linear(prior='mur')``).
+
+Measured behaviour: the fitted ghost maps predict the ghosts to about 10% RMS and, over the
+first pass of a pulse, leave an error some 30 dB below the same 2-cell layer without the
+network (zero ghosts); in closed-loop feedback every map fitted to the one-step targets so far
+develops an error that grows by a few percent per step after 250-500 steps, while Mur's map is
+stable at about -17 dB. None reaches -40 dB, so the judge rejects them and the simulation
+falls back to CPML.
 
 opencl_fdtd has no counterpart of this module: it absorbs with CPML only
 (opencl_fdtd/simulation.py:274-319).
@@ -120,6 +124,58 @@ def gather(shape, mask, E, H, X=None, R=None, C=None, stream=None):
     return X, R, C
 
 
+def _levi_civita(q, a, p):
+    return 1.0 if (q, a, p) in ((0, 1, 2), (1, 2, 0), (2, 0, 1)) else -1.0
+
+
+def _stencil_index(a, depth, offsets, comp):
+    """Input index of component ``comp`` at ``depth`` with tangential offsets {axis: -1|0|1}."""
+    ua, va = [r for r in range(3) if r != a]
+    return ((depth * 3 + offsets.get(ua, 0) + 1) * 3 + offsets.get(va, 0) + 1) * 6 + comp
+
+
+def mur_map(face: int, dt: float = DEFAULT_DT, memory: float = None):
+    """[109][6] linear map (rows: the 108 stencil inputs, then the bias) that, with the memory
+    term m = (1 - c dt) / (1 + c dt), gives Mur's first-order absorbing condition (Mur 1981,
+    IEEE Trans. EMC 23, one-way wave equation along the face normal, c = 1, unit cells) written
+    for the ghost fields:
+      side 0, H ghost:  G^{n+1/2} = m G^{n-1/2} + (1 - m) H_p(0)^{n+1/2} + dt (curl E^n)_p(0)
+      side 1, E ghost:  G^{n+1}   = m G^n       + (1 - m) E_p(s-1)^n      - m dt (curl H^{n+1/2})_p(s-1)
+    (H_p(0)^{n-1/2} and E_p(s-1)^{n+1}, which Mur's update needs, are the stencil's values
+    stepped back / forward by the Yee update, hence the curl terms; curls with forward
+    differences for E, backward for H, as the Yee updates take them). Being linear, the map is
+    the same on the normalised stencil."""
+    m = ((1.0 - dt) / (1.0 + dt)) if memory is None else memory
+    a, side = divmod(int(face), 2)
+    A = numpy.zeros((IN + 1, OUT))
+    for p in range(3):
+        if p == a:
+            continue
+        if side == 0:
+            o = 3 + p
+            A[_stencil_index(a, 0, {}, 3 + p), o] += 1.0 - m
+            for a2 in range(3):
+                for q2 in range(3):
+                    if len({p, a2, q2}) < 3:
+                        continue
+                    e = _levi_civita(p, a2, q2)
+                    plus = _stencil_index(a, 1, {}, q2) if a2 == a else _stencil_index(a, 0, {a2: 1}, q2)
+                    A[plus, o] += dt * e
+                    A[_stencil_index(a, 0, {}, q2), o] -= dt * e
+        else:
+            o = p
+            A[_stencil_index(a, 0, {}, p), o] += 1.0 - m
+            for a2 in range(3):
+                for q2 in range(3):
+                    if len({p, a2, q2}) < 3:
+                        continue
+                    e = _levi_civita(p, a2, q2)
+                    minus = _stencil_index(a, 1, {}, 3 + q2) if a2 == a else _stencil_index(a, 0, {a2: -1}, 3 + q2)
+                    A[_stencil_index(a, 0, {}, 3 + q2), o] -= m * dt * e
+                    A[minus, o] += m * dt * e
+    return A
+
+
 # ---------------------------------------------------------------------------------------------
 # the network and its training
 # ---------------------------------------------------------------------------------------------
@@ -127,10 +183,13 @@ class BoundaryNet:
     """Six per-face networks (face f = 2 * axis + side): float32 parameters [6][NPARAM] on the
     device with their Adam moments."""
 
-    def __init__(self, device=None, seed: int = 0, dt: float = DEFAULT_DT):
+    def __init__(self, device=None, seed: int = 0, dt: float = DEFAULT_DT, memory: float = 0.0):
         torch = _torch()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.dt = float(dt)
+        # weight of the previous step's ghost in each prediction (the teacher data's targets
+        # were formed with the same value)
+        self.memory = float(memory)
         rng = numpy.random.default_rng(seed)
         P = numpy.zeros((6, NPARAM), numpy.float32)
         for f in range(6):
@@ -264,16 +323,34 @@ class BoundaryNet:
             out += o.cpu().numpy().astype(numpy.float64).reshape(K + 1, N)
         return out
 
-    def fit_linear(self, data: "TeacherData", ridge: float = 1e-2, faces=range(6), bias_shift: float = 10.0):
-        """Start of training: the ridge least-squares linear map from the normalised stencils to
-        the weighted ghost components, embedded exactly in the network. Normal equations from
-        fdtd_gram on the device (X^T X in two column halves, X^T T), solved on the host in
-        float64 with ``ridge`` times the sample count added to the diagonal (the same as input
-        noise of variance ``ridge``: it keeps the boundary stable in feedback). The map enters
-        six hidden units of each layer with a bias shift that keeps GELU in its linear range
-        (gelu(a) = a Phi(a), Phi(a) > 1 - 1e-6 for a > 4.8), and the output bias removes the
-        shift; every other unit starts at zero. Returns {face: loss}."""
+    def embed_linear(self, face: int, A, bias_shift: float = 10.0):
+        """Put the [109][6] linear map A (rows: inputs, then bias) into the network exactly: six
+        hidden units per layer with a bias shift that keeps GELU in its linear range
+        (gelu(a) = a Phi(a), Phi(a) > 1 - 1e-6 for a > 4.8), the output bias removing the shift;
+        every other unit at zero."""
         torch = _torch()
+        P = numpy.zeros(NPARAM)
+        P[W1:B1].reshape(IN, HID)[:, :OUT] = A[:IN]
+        P[B1:B1 + OUT] = A[IN] + bias_shift
+        for o in range(OUT):
+            P[W2:B2].reshape(HID, HID)[o, o] = 1.0
+            P[W3:B3].reshape(HID, OUT)[o, o] = 1.0
+        P[B3:B3 + OUT] = -bias_shift
+        self.params[face] = torch.from_numpy(P.astype(numpy.float32)).to(self.device)
+        self.m[face].zero_()
+        self.v[face].zero_()
+        self.steps[face] = 0
+        self._packed = None
+
+    def fit_linear(self, data: "TeacherData", ridge: float = 1e-2, faces=range(6), prior: str = None):
+        """Start of training: the regularised least-squares linear map from the normalised
+        stencils to the weighted targets, embedded exactly in the network (``embed_linear``).
+        Normal equations from fdtd_gram on the device (X^T X in two column halves, X^T T),
+        solved on the host in float64: minimise |X A - T|^2 + ridge n |A - A0|^2 over the n
+        samples, A0 = 0 or, with prior='mur', Mur's first-order map (``mur_map``; the net's
+        memory must be Mur's). Shrinking towards Mur, whose layer is stable in feedback, keeps
+        the map stable for a large enough ridge; shrinking towards zero does not. Returns
+        {face: loss}."""
         out = {}
         for f in faces:
             X, T = data.X[f], data.T[f]
@@ -282,28 +359,18 @@ class BoundaryNet:
                 continue
             h = IN // 2
             G = numpy.zeros((IN + 1, IN + 1))
-            g0 = self.gram(X, X[:, :h])
-            g1 = self.gram(X, X[:, h:])
-            G[:, :h], G[:, h:IN] = g0, g1
+            G[:, :h] = self.gram(X, X[:, :h])
+            G[:, h:IN] = self.gram(X, X[:, h:])
             G[:IN, IN] = G[IN, :IN]
             G[IN, IN] = n
-            G[numpy.arange(IN), numpy.arange(IN)] += ridge * n
             XT = self.gram(X, T)
-            A = numpy.linalg.solve(G, XT)                       # [109][6]
+            A0 = mur_map(f, self.dt, self.memory) if prior == "mur" else numpy.zeros((IN + 1, OUT))
+            R = numpy.zeros((IN + 1, IN + 1))
+            R[numpy.arange(IN), numpy.arange(IN)] = ridge * n
+            A = numpy.linalg.solve(G + R, XT + R @ A0)
             w = self.output_weights(f).cpu().numpy()
             A[:, w == 0] = 0.0
-            P = numpy.zeros(NPARAM)
-            P[W1:B1].reshape(IN, HID)[:, :OUT] = A[:IN]
-            P[B1:B1 + OUT] = A[IN] + bias_shift
-            for o in range(OUT):
-                P[W2:B2].reshape(HID, HID)[o, o] = 1.0
-                P[W3:B3].reshape(HID, OUT)[o, o] = 1.0
-            P[B3:B3 + OUT] = -bias_shift
-            self.params[f] = torch.from_numpy(P.astype(numpy.float32)).to(self.device)
-            self.m[f].zero_()
-            self.v[f].zero_()
-            self.steps[f] = 0
-            self._packed = None
+            self.embed_linear(f, A)
             out[f] = self.loss(f, X, T)
         return out
 
@@ -330,23 +397,25 @@ class BoundaryNet:
         return self._packed
 
     def state_dict(self) -> dict:
-        return {"params": self.params.detach().cpu().numpy(), "dt": self.dt}
+        return {"params": self.params.detach().cpu().numpy(), "dt": self.dt, "memory": self.memory}
 
     def load_state_dict(self, st: dict):
         torch = _torch()
         self.params.copy_(torch.as_tensor(numpy.asarray(st["params"], numpy.float32)).to(self.device))
         self.dt = float(st.get("dt", self.dt))
+        self.memory = float(st.get("memory", self.memory))
         self._packed = None
 
     def save(self, path):
         st = self.state_dict()
-        numpy.savez(path, params=st["params"], dt=numpy.float64(st["dt"]))
+        numpy.savez(path, params=st["params"], dt=numpy.float64(st["dt"]), memory=numpy.float64(st["memory"]))
 
     @classmethod
     def load(cls, path, device=None):
         z = numpy.load(path)
-        net = cls(device=device, dt=float(z["dt"]))
-        net.load_state_dict({"params": z["params"], "dt": float(z["dt"])})
+        memory = float(z["memory"]) if "memory" in z.files else 0.0
+        net = cls(device=device, dt=float(z["dt"]), memory=memory)
+        net.load_state_dict({"params": z["params"], "dt": float(z["dt"]), "memory": memory})
         return net
 
 
@@ -474,7 +543,7 @@ def sphere_epsilon_inside(shape, n, seed, lo, hi, eps_range=(1.0, 12.0), r_range
 
 def teacher_run(data: TeacherData, seed: int, size: int = 128, cpml: int = 16, steps: int = 1500,
                 every: int = 25, per_face: int = 512, dt: float = DEFAULT_DT, period_range=(10.0, 30.0),
-                spheres=(1, 8), rel_threshold: float = 1e-3, face_margin: int = 4):
+                spheres=(1, 8), rel_threshold: float = 1e-3, face_margin: int = 4, memory: float = 0.0):
     """One plain run with a ``cpml``-cell CPML on every face of a size^3 grid; at every
     ``every``-th step adds training pairs of its interior box (size - 2 cpml)^3 to ``data``:
     stencils of the pre-step state E^n, H^{n+1/2}; targets the teacher's fields one cell outside
@@ -482,7 +551,9 @@ def teacher_run(data: TeacherData, seed: int, size: int = 128, cpml: int = 16, s
     the side-1 faces. The dielectric spheres stay ``face_margin`` cells inside the box, so the
     learned faces see a homogeneous exterior. Columns whose stencil RMS is below
     ``rel_threshold`` times the largest seen so far in the run are skipped, at most ``per_face``
-    random columns of a face are kept per sample. Returns the box shape."""
+    random columns of a face are kept per sample. With ``memory`` m the targets are the ghosts
+    minus m times the previous step's ghosts (the step before each sample is made by hand too).
+    Returns the box shape."""
     torch = _torch()
     from .simulation import Simulation
     rng = numpy.random.default_rng(seed)
@@ -507,28 +578,46 @@ def teacher_run(data: TeacherData, seed: int, size: int = 128, cpml: int = 16, s
     gen.manual_seed(int(seed))
     keep = [0.0, float(rel_threshold)]
     _, off = columns(box, FACES_ALL)
+    lead = 2 if memory else 1
     t = 0
     while t < steps:
-        n = min(every - 1, steps - t) if every > 1 else 0
+        n = min(every - lead, steps - t) if every > lead else 0
         if n > 0:
             sim.run(n, point_sources=[(k * N + cell, values[k][t:t + n]) for k in range(3)])
             t += n
-        if t >= steps:
+        if t + lead > steps:
             break
+        prev = {}
+        if memory:
+            # the step before the sample, by hand: its ghosts are the memory term's inputs
+            for a in range(3):
+                prev[2 * a] = _ghost_plane(sim.H, shape, pad, box, a, 0).clone()
+            sim.update_E()
+            for k in range(3):
+                sim.E[k * N + cell] += numpy.float32(values[k][t])
+            for a in range(3):
+                prev[2 * a + 1] = _ghost_plane(sim.E, shape, pad, box, a, 1).clone()
+            sim.update_H()
+            sim.steps_run += 1
+            t += 1
         # one step by hand: stencils before it, H ghosts now, E ghosts after the E update
         X, R, _ = gather(box, FACES_ALL, _box(sim.E, shape, pad), _box(sim.H, shape, pad))
         sel = _select(R, off, box, gen, per_face, keep)
         for f, idx in sel.items():
             if f % 2 == 0:
-                g = _ghost_plane(sim.H, shape, pad, box, f // 2, 0)
-                data.add(f, X[off[f] + idx], _six(g[idx], "H") / R[off[f] + idx, None])
+                g = _ghost_plane(sim.H, shape, pad, box, f // 2, 0)[idx]
+                if memory:
+                    g = g - memory * prev[f][idx]
+                data.add(f, X[off[f] + idx], _six(g, "H") / R[off[f] + idx, None])
         sim.update_E()
         for k in range(3):
             sim.E[k * N + cell] += numpy.float32(values[k][t])
         for f, idx in sel.items():
             if f % 2 == 1:
-                g = _ghost_plane(sim.E, shape, pad, box, f // 2, 1)
-                data.add(f, X[off[f] + idx], _six(g[idx], "E") / R[off[f] + idx, None])
+                g = _ghost_plane(sim.E, shape, pad, box, f // 2, 1)[idx]
+                if memory:
+                    g = g - memory * prev[f][idx]
+                data.add(f, X[off[f] + idx], _six(g, "E") / R[off[f] + idx, None])
         sim.update_H()
         sim.steps_run += 1
         t += 1
@@ -567,6 +656,7 @@ class LearnedBoundary:
         self.precision = precision
         self.mask = face_mask(faces)
         self._attached = {}
+        self._pred = {}
 
     def _check(self, sim):
         if numpy.dtype(sim.arg_type) != numpy.float32:
@@ -585,28 +675,34 @@ class LearnedBoundary:
         torch = _torch()
         self._check(sim)
         ncol, _ = columns(sim.shape, self.mask)
-        pred = torch.empty(max(ncol, 1) * OUT, dtype=torch.float32, device=sim.device)
+        pred = torch.zeros(max(ncol, 1) * OUT, dtype=torch.float32, device=sim.device)
         W = self.net.weights(self.precision)
-        _lib.check(sim._lib.fdtd_lbc_attach(sim._plan, self.mask, PRECISIONS[self.precision], W.data_ptr(),
+        _lib.check(sim._lib.fdtd_lbc_attach(sim._plan, self.mask, PRECISIONS[self.precision], self.net.memory,
+                                            W.data_ptr(),
                                             pred.data_ptr(), pred.numel()))
         self._attached[id(sim)] = (sim, pred, W)
         return sim
 
     def detach(self, sim):
-        _lib.check(sim._lib.fdtd_lbc_attach(sim._plan, 0, 0, None, None, 0))
+        _lib.check(sim._lib.fdtd_lbc_attach(sim._plan, 0, 0, 0.0, None, None, 0))
         self._attached.pop(id(sim), None)
 
     def predict(self, sim, side: int = -1, pred=None, stream=None):
         """Ghost values [ncol][6] of the faces of ``side`` (-1: all) from sim's current state
-        (for stepping with update_E / update_H)."""
+        (for stepping with update_E / update_H). With a memory term the previous ghosts are
+        read from ``pred`` (default: a buffer kept per simulation, zero at first)."""
         torch = _torch()
         ncol, _ = columns(sim.shape, self.mask)
-        pred = torch.zeros((ncol, OUT), dtype=torch.float32, device=sim.device) if pred is None else pred
+        if pred is None:
+            pred = self._pred.get(id(sim))
+            if pred is None or pred.shape[0] != ncol:
+                pred = torch.zeros((ncol, OUT), dtype=torch.float32, device=sim.device)
+                self._pred[id(sim)] = pred
         st = stream or sim.queue
         W = self.net.weights(self.precision)
         _lib.check(sim._lib.fdtd_lbc_predict(_shape_arg(sim.shape), self.mask, int(side), PRECISIONS[self.precision],
-                                             W.data_ptr(), sim.E.data_ptr(), sim.H.data_ptr(), pred.data_ptr(),
-                                             pred.numel(), ctypes.c_void_p(st.cuda_stream)))
+                                             self.net.memory, W.data_ptr(), sim.E.data_ptr(), sim.H.data_ptr(),
+                                             pred.data_ptr(), pred.numel(), ctypes.c_void_p(st.cuda_stream)))
         return pred
 
     def fix(self, sim, pred, fields: str, stream=None):
@@ -763,15 +859,22 @@ def thin_or_cpml(kwargs: dict, boundary: LearnedBoundary, judged_db: float = Non
     return Simulation(**kw), "cpml"
 
 
-def train(runs: int = 200, seed: int = 0, ridge: float = 1e-2, finetune_iters: int = 1000,
-          finetune_lr: float = 1e-4, input_noise: float = 0.1, device=None, **teacher_kw):
-    """The training pipeline: ``runs`` teacher runs (``teacher_run``), the ridge least-squares
-    start (``BoundaryNet.fit_linear``) and an Adam fine-tune with input noise
+MUR_MEMORY = (1.0 - DEFAULT_DT) / (1.0 + DEFAULT_DT)   # -(c dt - dx) / (c dt + dx), vacuum, unit cells
+
+
+def train(runs: int = 200, seed: int = 0, ridge: float = 1.0, finetune_iters: int = 0,
+          finetune_lr: float = 1e-4, input_noise: float = 0.1, device=None, memory: float = None,
+          prior: str = "mur", data=None, **teacher_kw):
+    """The training pipeline: ``runs`` teacher runs (``teacher_run``, targets formed with the
+    memory term, Mur's by default), the regularised least-squares start shrunk towards
+    ``prior`` (``BoundaryNet.fit_linear``) and an optional Adam fine-tune with input noise
     (``BoundaryNet.fit``). Returns (net, data, {face: loss after the start},
     {face: loss after the fine-tune})."""
-    data = make_teacher_data(runs=runs, seed=seed, device=device, **teacher_kw)
-    net = BoundaryNet(device=device, seed=seed + 1)
-    start = net.fit_linear(data, ridge=ridge)
+    memory = MUR_MEMORY if memory is None else memory
+    if data is None:
+        data = make_teacher_data(runs=runs, seed=seed, device=device, memory=memory, **teacher_kw)
+    net = BoundaryNet(device=device, seed=seed + 1, memory=memory)
+    start = net.fit_linear(data, ridge=ridge, prior=prior)
     fin = net.fit(data, iters=finetune_iters, batch=4096, lr=finetune_lr, lr_final=finetune_lr * 1e-2,
                   input_noise=input_noise) if finetune_iters > 0 else dict(start)
     return net, data, start, fin

@@ -113,12 +113,12 @@ def test_adam_matches_oracle():
     assert net.steps == [0, 3, 0, 0, 0, 0]
 
 
-def _predict(L, shape, mask, precision, W, E, H, side=-1):
+def _predict(L, shape, mask, precision, W, E, H, side=-1, memory=0.0, prev=None):
     n, _ = L.columns(shape, mask)
-    pred = torch.zeros((n, 6), dtype=torch.float32, device="cuda")
+    pred = torch.zeros((n, 6), dtype=torch.float32, device="cuda") if prev is None else _cuda(prev)
     lib = L._lib.load()
-    L._lib.check(lib.fdtd_lbc_predict(L._shape_arg(shape), mask, side, L.PRECISIONS[precision], W.data_ptr(),
-                                      E.data_ptr(), H.data_ptr(), pred.data_ptr(), pred.numel(),
+    L._lib.check(lib.fdtd_lbc_predict(L._shape_arg(shape), mask, side, L.PRECISIONS[precision], memory,
+                                      W.data_ptr(), E.data_ptr(), H.data_ptr(), pred.data_ptr(), pred.numel(),
                                       ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
     return pred.cpu().numpy()
 
@@ -158,6 +158,27 @@ def test_predict_tensor_cores_match_float32(shape):
         _, face_of = O.column_cells(shape, 63)
         assert not p0[face_of % 2 == 1].any()
         numpy.testing.assert_array_equal(p0[face_of % 2 == 0], p[face_of % 2 == 0])
+
+
+@pytest.mark.parametrize("precision", ["f32", "bf16", "bf16x2"])
+def test_predict_memory_term(precision):
+    """pred = r * net + memory * (previous pred), rows of the other side untouched."""
+    L = _L()
+    shape = (10, 9, 8)
+    net = _net(40, 200.0)
+    net.params.copy_(net.params.to(torch.bfloat16).to(torch.float32))
+    net._packed = None
+    E, H = _fields(shape, 41, 0.05)
+    Ed, Hd = _cuda(E), _cuda(H)
+    W = net.weights(precision)
+    n, _ = L.columns(shape)
+    prev = numpy.random.default_rng(42).standard_normal((n, 6)).astype(numpy.float32)
+    p0 = _predict(L, shape, 63, precision, W, Ed, Hd)
+    p1 = _predict(L, shape, 63, precision, W, Ed, Hd, memory=0.27, prev=prev)
+    numpy.testing.assert_allclose(p1, p0 + numpy.float32(0.27) * prev, rtol=1e-5, atol=1e-6)
+    _, face_of = O.column_cells(shape, 63)
+    p2 = _predict(L, shape, 63, precision, W, Ed, Hd, side=1, memory=0.5, prev=prev)
+    numpy.testing.assert_array_equal(p2[face_of % 2 == 0], prev[face_of % 2 == 0])
 
 
 @pytest.mark.parametrize("mask,fields", [(63, "E"), (63, "H"), (0b011011, "H"), (0b110100, "E")])
@@ -239,12 +260,13 @@ def _sim_kwargs(shape, seed, poynting=False):
                 dt=0.99 / math.sqrt(3))
 
 
-@pytest.mark.parametrize("precision", ["f32", "bf16", "bf16x2"])
-def test_run_with_boundary_equals_manual_steps(precision):
+@pytest.mark.parametrize("precision,memory", [("f32", 0.0), ("bf16", 0.27), ("bf16x2", 0.0)])
+def test_run_with_boundary_equals_manual_steps(precision, memory):
     from opencl_fdtd_gb300 import Simulation
     L = _L()
     shape = (16, 12, 10)
     net = _net(11, 50.0)
+    net.memory = memory
     lb = L.LearnedBoundary(net, precision)
     a = Simulation(**_sim_kwargs(shape, 12))
     b = Simulation(**_sim_kwargs(shape, 12))
