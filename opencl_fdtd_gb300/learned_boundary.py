@@ -42,12 +42,12 @@ Memory term: a ghost is predicted as r * MLP(x) + memory * (the previous step's 
 memory = (1 - c dt) / (1 + c dt) the form contains Mur's first-order absorbing condition
 (``mur_map``), and training can shrink the fitted map towards Mur's (``fit_linear(prior='mur')``).
 
-Measured behaviour: the fitted ghost maps predict the ghosts to about 10% RMS and, over the
-first pass of a pulse, leave an error some 30 dB below the same 2-cell layer without the
-network (zero ghosts); in closed-loop feedback every map fitted to the one-step targets so far
-develops an error that grows by a few percent per step after 250-500 steps, while Mur's map is
-stable at about -17 dB. None reaches -40 dB, so the judge rejects them and the simulation
-falls back to CPML.
+Measured behaviour: fitted on the full 108-value stencil, the ghost maps predict the ghosts to
+about 10% RMS and, over the first pass of a pulse, leave an error some 30 dB below the same
+2-cell layer without the network (zero ghosts), but in closed-loop feedback they grow after
+250-500 steps; fitted on Mur's stencil only (``fit_linear(support='mur')``) the layer is
+stable and beats Mur's own coefficients (-22 against -18 dB in the training band). None
+reaches -40 dB, so the judge rejects them and the simulation falls back to CPML.
 
 opencl_fdtd has no counterpart of this module: it absorbs with CPML only
 (opencl_fdtd/simulation.py:274-319).
@@ -342,15 +342,18 @@ class BoundaryNet:
         self.steps[face] = 0
         self._packed = None
 
-    def fit_linear(self, data: "TeacherData", ridge: float = 1e-2, faces=range(6), prior: str = None):
+    def fit_linear(self, data: "TeacherData", ridge: float = 1e-2, faces=range(6), prior: str = None,
+                   support: str = None):
         """Start of training: the regularised least-squares linear map from the normalised
         stencils to the weighted targets, embedded exactly in the network (``embed_linear``).
         Normal equations from fdtd_gram on the device (X^T X in two column halves, X^T T),
         solved on the host in float64: minimise |X A - T|^2 + ridge n |A - A0|^2 over the n
         samples, A0 = 0 or, with prior='mur', Mur's first-order map (``mur_map``; the net's
         memory must be Mur's). Shrinking towards Mur, whose layer is stable in feedback, keeps
-        the map stable for a large enough ridge; shrinking towards zero does not. Returns
-        {face: loss}."""
+        the map stable for a large enough ridge; shrinking towards zero does not. ``support``
+        limits each output to some inputs: 'mur' to the inputs Mur's map uses for it, 'mur3x3'
+        to the components those inputs carry at every tangential position of both depths.
+        Returns {face: loss}."""
         out = {}
         for f in faces:
             X, T = data.X[f], data.T[f]
@@ -367,7 +370,21 @@ class BoundaryNet:
             A0 = mur_map(f, self.dt, self.memory) if prior == "mur" else numpy.zeros((IN + 1, OUT))
             R = numpy.zeros((IN + 1, IN + 1))
             R[numpy.arange(IN), numpy.arange(IN)] = ridge * n
-            A = numpy.linalg.solve(G + R, XT + R @ A0)
+            if support is None:
+                A = numpy.linalg.solve(G + R, XT + R @ A0)
+            else:
+                Am = mur_map(f, self.dt, self.memory)
+                A = numpy.zeros((IN + 1, OUT))
+                for o in range(OUT):
+                    rows = numpy.flatnonzero(Am[:IN, o])
+                    if rows.size == 0:
+                        continue
+                    if support == "mur3x3":
+                        comps = sorted(set(int(r) % 6 for r in rows))
+                        rows = numpy.array([k for k in range(IN) if k % 6 in comps])
+                    idx = numpy.append(rows, IN)                 # and the bias
+                    Gs = (G + R)[numpy.ix_(idx, idx)]
+                    A[idx, o] = numpy.linalg.solve(Gs, (XT + R @ A0)[idx, o])
             w = self.output_weights(f).cpu().numpy()
             A[:, w == 0] = 0.0
             self.embed_linear(f, A)
