@@ -633,7 +633,7 @@ def run_c4(args):
     plain_E = [s.E.clone() for s in sims]
     plain_series = [m.series()[:, 0] for m in mons]
     results = {}
-    for storage in ("f32", "bf16", "fp16"):
+    for storage in ("f32", "bf16", "fp16", "bf16u"):
         reset()
         b = BatchSimulation(sims, storage=storage, sources=sources, monitors=monitors, steps=steps)
         tune = b.autotune(steps=10)
@@ -656,7 +656,7 @@ def run_c4(args):
         numpy.array_equal(a, c) for a, c in zip(plain_series, results["f32"]["series"]))
     # float64 reference of every variant: errors of the float32 and 16-bit runs
     w0 = 2 * math.pi * 40.0 / 1550.0
-    err = {k: {"rel_l2": [], "peak_rel": []} for k in ("f32", "bf16", "fp16")}
+    err = {k: {"rel_l2": [], "peak_rel": []} for k in ("f32", "bf16", "fp16", "bf16u")}
     for v, var in enumerate(variants):
         kw64, ind = workloads.c4_kwargs(var, float_type=numpy.float64)
         s64 = Simulation(**kw64)
@@ -683,7 +683,7 @@ def run_c4(args):
     line = {
         "metric": METRIC, "value": best["value"], "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": 10,
         "ms_per_step": round(best["ms"] / steps, 5), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 arithmetic; f32 / bf16 / fp16 storage", "data": "synthetic (seeded L3 variants)",
+        "vs_baseline": None, "dtype": "f32 arithmetic; f32 / bf16 / fp16 / bf16 (no tile exponents) storage", "data": "synthetic (seeded L3 variants)",
         "config": {"workload": "c4: %d seeded L3-cavity variants, grids U{96..256}xU{96..224}xU{48..73}, "
                                "a ~ U[8,12], r ~ U[0.25a,0.35a], 8-cell CPML x6, Poynting off, %d steps"
                                % (len(variants), steps),

@@ -240,10 +240,13 @@ int fdtd_run_kernel_ms(const FdtdPlan *plan, double ms[2], int32_t *samples);
  * consecutive (y, z) cells of one component in one x plane carries a power-of-two exponent e
  * (stored = value * 2^-e), chosen when the run is written. e_exp / h_exp are int32
  * [sx][ceil(sy*sz/32)]: one word per run holds the three components' exponents as the bytes
- * e_c + 128 at bits 8c .. 8c + 7. */
+ * e_c + 128 at bits 8c .. 8c + 7. FDTD_STORE_BF16U stores bfloat16 without exponents
+ * (bfloat16 has float32's exponent range, so a tile exponent changes none of its roundings
+ * short of the subnormal range) and takes no e_exp / h_exp. */
 #define FDTD_STORE_F32 0
 #define FDTD_STORE_BF16 1
 #define FDTD_STORE_F16 2
+#define FDTD_STORE_BF16U 3
 #define FDTD_BATCH_MAX_SRC 4
 #define FDTD_BATCH_MAX_MON 8
 

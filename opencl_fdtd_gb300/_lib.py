@@ -72,7 +72,7 @@ class FdtdDftMonitor(ctypes.Structure):
                 ("accum", c_vp), ("series", c_vp), ("step", c_i64), ("series_row", c_i64)]
 
 
-FDTD_STORE_F32, FDTD_STORE_BF16, FDTD_STORE_F16 = 0, 1, 2
+FDTD_STORE_F32, FDTD_STORE_BF16, FDTD_STORE_F16, FDTD_STORE_BF16U = 0, 1, 2, 3
 FDTD_BATCH_MAX_SRC, FDTD_BATCH_MAX_MON = 4, 8
 FDTD_BATCH_PERSISTENT, FDTD_BATCH_LAUNCHES = 0, 1
 

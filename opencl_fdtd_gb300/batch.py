@@ -11,8 +11,10 @@ counter lives on the device.
 Storage: ``'f32'`` updates the simulations' own tensors in place (results are bit-identical
 to ``Simulation.run`` of each variant). ``'bf16'`` / ``'fp16'`` keep E, H and dt/eps in 16-bit
 copies owned here, with a power-of-two exponent per run of 32 cells of one component in one
-x plane (arithmetic stays float32, CPML psi float32); ``sync()`` decodes them back into the
-simulations' E and H. Point sources and monitor points are given per variant when the batch
+x plane (arithmetic stays float32, CPML psi float32); ``'bf16u'`` keeps bfloat16 copies
+without the exponents (bfloat16 has float32's exponent range, so the exponents change no
+rounding there short of subnormals, and the codec's warp reductions go); ``sync()`` decodes
+the copies back into the simulations' E and H. Point sources and monitor points are given per variant when the batch
 is built: sources as the flat index into E and one value per step, monitors as flat indices
 whose E values are recorded after every step's sources (float64 series).
 """
@@ -24,7 +26,8 @@ import numpy
 
 from . import _lib
 
-_STORE = {"f32": _lib.FDTD_STORE_F32, "bf16": _lib.FDTD_STORE_BF16, "fp16": _lib.FDTD_STORE_F16}
+_STORE = {"f32": _lib.FDTD_STORE_F32, "bf16": _lib.FDTD_STORE_BF16, "fp16": _lib.FDTD_STORE_F16,
+          "bf16u": _lib.FDTD_STORE_BF16U}
 
 
 class BatchSimulation:
@@ -34,7 +37,7 @@ class BatchSimulation:
         source and monitor arrays (steps past it add no source and record nothing)."""
         import torch
         if storage not in _STORE:
-            raise ValueError("storage must be 'f32', 'bf16' or 'fp16'")
+            raise ValueError("storage must be 'f32', 'bf16', 'fp16' or 'bf16u'")
         if not sims:
             raise ValueError("no simulations")
         self.sims = list(sims)
@@ -54,7 +57,8 @@ class BatchSimulation:
         self.series = []
         self._e16, self._h16, self._eexp, self._hexp = [], [], [], []
         arr = (_lib.FdtdBatchVariant * n)()
-        half = {"bf16": torch.bfloat16, "fp16": torch.float16}.get(storage)
+        half = {"bf16": torch.bfloat16, "fp16": torch.float16, "bf16u": torch.bfloat16}.get(storage)
+        scaled = storage in ("bf16", "fp16")
         for v, sim in enumerate(self.sims):
             if sim._np_dtype != numpy.float32:
                 raise ValueError("batched stepping needs float32 simulations")
@@ -86,15 +90,16 @@ class BatchSimulation:
                 e16 = torch.empty(3 * sim.N, dtype=half, device=dev)
                 h16 = torch.empty(3 * sim.N, dtype=half, device=dev)
                 ce16 = sim._ce.to(half)
-                eexp = torch.zeros(sim.shape[0] * ntl, dtype=torch.int32, device=dev)
-                hexp = torch.zeros_like(eexp)
                 self._keep.append(ce16)
                 self._e16.append(e16)
                 self._h16.append(h16)
-                self._eexp.append(eexp)
-                self._hexp.append(hexp)
                 d.E, d.H, d.ce = e16.data_ptr(), h16.data_ptr(), ce16.data_ptr()
-                d.e_exp, d.h_exp = eexp.data_ptr(), hexp.data_ptr()
+                if scaled:
+                    eexp = torch.zeros(sim.shape[0] * ntl, dtype=torch.int32, device=dev)
+                    hexp = torch.zeros_like(eexp)
+                    self._eexp.append(eexp)
+                    self._hexp.append(hexp)
+                    d.e_exp, d.h_exp = eexp.data_ptr(), hexp.data_ptr()
             src = list(sources[v])
             if len(src) > _lib.FDTD_BATCH_MAX_SRC:
                 raise ValueError("at most %d point sources per variant" % _lib.FDTD_BATCH_MAX_SRC)

@@ -62,6 +62,14 @@ struct Store<BATCH_F16> {
     __device__ static T enc(float v) { return __float2half_rn(v); }
 };
 
+template <>
+struct Store<BATCH_BF16U> {
+    using T = __nv_bfloat16;
+    static constexpr bool scaled = false;
+    __device__ static float dec(T v) { return __bfloat162float(v); }
+    __device__ static T enc(float v) { return __float2bfloat16_rn(v); }
+};
+
 // 2^e for e in [-126, 127] (exact)
 __device__ __forceinline__ float pow2(int e) { return __int_as_float((e + 127) << 23); }
 
@@ -515,15 +523,15 @@ __global__ void __launch_bounds__(BATCH_THREADS) k_batch_encode(const BVar v, in
     float val[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) val[c] = act ? src[(uint64_t)c * v.N + i] : 0.f;
-    int e[3];
-    warp_exps(val[0], val[1], val[2], e[0], e[1], e[2]);
+    int e[3] = {0, 0, 0};
+    if (SS::scaled) warp_exps(val[0], val[1], val[2], e[0], e[1], e[2]);
     T *dst = (T *)(field ? v.H : v.E);
     if (act) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) dst[(uint64_t)c * v.N + i] = SS::enc(val[c] * pow2(-e[c]));
+        for (int c = 0; c < 3; ++c) dst[(uint64_t)c * v.N + i] = SS::enc(SS::scaled ? val[c] * pow2(-e[c]) : val[c]);
     }
     const uint32_t jt = j / BATCH_TILE;
-    if ((threadIdx.x & 31u) == 0 && jt < v.ntl)
+    if (SS::scaled && (threadIdx.x & 31u) == 0 && jt < v.ntl)
         (field ? v.hexp : v.eexp)[texp_index(v, x, jt)] = xpack(e[0], e[1], e[2]);
 }
 
@@ -537,9 +545,9 @@ __global__ void __launch_bounds__(BATCH_THREADS) k_batch_decode(const BVar v, in
     if (j >= v.syz) return;
     const uint64_t i = (uint64_t)x * v.syz + j;
     const T *src = (const T *)(field ? v.H : v.E);
-    const int32_t w = (field ? v.hexp : v.eexp)[texp_index(v, x, j / BATCH_TILE)];
+    const int32_t w = SS::scaled ? (field ? v.hexp : v.eexp)[texp_index(v, x, j / BATCH_TILE)] : 0;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) dst[(uint64_t)c * v.N + i] = SS::dec(src[(uint64_t)c * v.N + i]) * pow2(xe(w, c));
+    for (int c = 0; c < 3; ++c) dst[(uint64_t)c * v.N + i] = dv<ST>(src[(uint64_t)c * v.N + i], xe(w, c));
 }
 
 }  // namespace
@@ -583,6 +591,7 @@ cudaError_t launch_batch_encode(int store, const BVar &v, int field, const float
     const dim3 g(v.njb, v.sx, 1);
     if (store == BATCH_BF16) k_batch_encode<BATCH_BF16><<<g, BATCH_THREADS, 0, st>>>(v, field, src);
     else if (store == BATCH_F16) k_batch_encode<BATCH_F16><<<g, BATCH_THREADS, 0, st>>>(v, field, src);
+    else if (store == BATCH_BF16U) k_batch_encode<BATCH_BF16U><<<g, BATCH_THREADS, 0, st>>>(v, field, src);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
@@ -592,6 +601,7 @@ cudaError_t launch_batch_decode(int store, const BVar &v, int field, float *dst,
     const dim3 g(v.njb, v.sx, 1);
     if (store == BATCH_BF16) k_batch_decode<BATCH_BF16><<<g, BATCH_THREADS, 0, st>>>(v, field, dst);
     else if (store == BATCH_F16) k_batch_decode<BATCH_F16><<<g, BATCH_THREADS, 0, st>>>(v, field, dst);
+    else if (store == BATCH_BF16U) k_batch_decode<BATCH_BF16U><<<g, BATCH_THREADS, 0, st>>>(v, field, dst);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
@@ -605,5 +615,8 @@ template cudaError_t launch_batch_steps<BATCH_F16>(const BatchK &, cudaStream_t)
 template int batch_max_blocks_per_sm<BATCH_F32>();
 template int batch_max_blocks_per_sm<BATCH_BF16>();
 template int batch_max_blocks_per_sm<BATCH_F16>();
+template cudaError_t launch_batch<BATCH_BF16U>(const BatchK &, int, cudaStream_t);
+template cudaError_t launch_batch_steps<BATCH_BF16U>(const BatchK &, cudaStream_t);
+template int batch_max_blocks_per_sm<BATCH_BF16U>();
 
 }  // namespace fdtd

@@ -18,6 +18,7 @@ constexpr int BATCH_MAX_MON = 8;
 constexpr int BATCH_F32 = 0;
 constexpr int BATCH_BF16 = 1;
 constexpr int BATCH_F16 = 2;
+constexpr int BATCH_BF16U = 3;     // bfloat16 without tile exponents (its exponent range is float32's)
 
 // CPML faces of one axis of one variant: tables [E/H][n/p][p0,p1,p2], psi [E/H][n/p][u/v]
 // (float32, updated in place). Tp = 0 when the 'p' face never applies.

@@ -8,6 +8,10 @@
 #include "fdtd_plan.h"
 #include "batch.h"
 
+static_assert(FDTD_STORE_F32 == fdtd::BATCH_F32 && FDTD_STORE_BF16 == fdtd::BATCH_BF16 &&
+                  FDTD_STORE_F16 == fdtd::BATCH_F16 && FDTD_STORE_BF16U == fdtd::BATCH_BF16U,
+              "storage codes");
+
 using namespace fdtd;
 
 struct FdtdBatch {
@@ -71,10 +75,11 @@ int make_var(const FdtdBatchVariant &d, int storage, BVar &v, int idx)
     v.E = d.E;
     v.H = d.H;
     v.ce = d.ce;
-    if (storage != BATCH_F32 && (!d.e_exp || !d.h_exp))
-        return fail(FDTD_ERR_INVALID, who + "16-bit storage needs e_exp and h_exp");
-    v.eexp = storage != BATCH_F32 ? d.e_exp : nullptr;
-    v.hexp = storage != BATCH_F32 ? d.h_exp : nullptr;
+    const bool scaled = storage == BATCH_BF16 || storage == BATCH_F16;
+    if (scaled && (!d.e_exp || !d.h_exp))
+        return fail(FDTD_ERR_INVALID, who + "16-bit storage with tile exponents needs e_exp and h_exp");
+    v.eexp = scaled ? d.e_exp : nullptr;
+    v.hexp = scaled ? d.h_exp : nullptr;
     if (d.n_pml < 0 || d.n_pml > 6) return fail(FDTD_ERR_INVALID, who + "n_pml must be in [0, 6]");
     int seen = 0;
     uint32_t tn[3] = {0, 0, 0}, tp[3] = {0, 0, 0};
@@ -139,6 +144,7 @@ int max_blocks(int storage)
 {
     if (storage == BATCH_BF16) return batch_max_blocks_per_sm<BATCH_BF16>();
     if (storage == BATCH_F16) return batch_max_blocks_per_sm<BATCH_F16>();
+    if (storage == BATCH_BF16U) return batch_max_blocks_per_sm<BATCH_BF16U>();
     return batch_max_blocks_per_sm<BATCH_F32>();
 }
 
@@ -152,8 +158,8 @@ int fdtd_batch_create(const FdtdBatchVariant *vars, int32_t n, int32_t storage, 
     if (!out) return fail(FDTD_ERR_INVALID, "fdtd_batch_create: out is NULL");
     *out = nullptr;
     if (!vars || n < 1) return fail(FDTD_ERR_INVALID, "fdtd_batch_create: no variants");
-    if (storage != BATCH_F32 && storage != BATCH_BF16 && storage != BATCH_F16)
-        return fail(FDTD_ERR_INVALID, "fdtd_batch_create: storage must be FDTD_STORE_F32, _BF16 or _F16");
+    if (storage != BATCH_F32 && storage != BATCH_BF16 && storage != BATCH_F16 && storage != BATCH_BF16U)
+        return fail(FDTD_ERR_INVALID, "fdtd_batch_create: storage must be FDTD_STORE_F32, _BF16, _F16 or _BF16U");
     if (rows < 0) return fail(FDTD_ERR_INVALID, "fdtd_batch_create: rows must be >= 0");
     FdtdBatch *b = new FdtdBatch();
     b->storage = storage;
@@ -226,11 +232,13 @@ int fdtd_batch_run(FdtdBatch *b, void *stream, int32_t nsteps)
     if (b->schedule == FDTD_BATCH_LAUNCHES) {
         if (b->storage == BATCH_BF16) e = launch_batch_steps<BATCH_BF16>(k, st);
         else if (b->storage == BATCH_F16) e = launch_batch_steps<BATCH_F16>(k, st);
+        else if (b->storage == BATCH_BF16U) e = launch_batch_steps<BATCH_BF16U>(k, st);
         else e = launch_batch_steps<BATCH_F32>(k, st);
         return check_cuda(e, "batch launch");
     }
     if (b->storage == BATCH_BF16) e = launch_batch<BATCH_BF16>(k, per * nsm, st);
     else if (b->storage == BATCH_F16) e = launch_batch<BATCH_F16>(k, per * nsm, st);
+    else if (b->storage == BATCH_BF16U) e = launch_batch<BATCH_BF16U>(k, per * nsm, st);
     else e = launch_batch<BATCH_F32>(k, per * nsm, st);
     return check_cuda(e, "batch launch");
 }

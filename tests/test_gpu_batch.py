@@ -99,7 +99,7 @@ def test_batch_graph_replay_equals_run():
         _same(x, y)
 
 
-@pytest.mark.parametrize("storage,tol", [("bf16", 5e-2), ("fp16", 1e-2)])
+@pytest.mark.parametrize("storage,tol", [("bf16", 5e-2), ("fp16", 1e-2), ("bf16u", 5e-2)])
 def test_batch_16bit_storage_tracks_f32(storage, tol):
     from opencl_fdtd_gb300.batch import BatchSimulation
     kws = [_variant(s, T, 50 + i) for i, (s, T) in enumerate(SHAPES[:3])]
@@ -119,7 +119,7 @@ def test_batch_16bit_storage_tracks_f32(storage, tol):
             assert err < tol, (storage, k, float(err))
 
 
-@pytest.mark.parametrize("storage,bits", [("bf16", 8), ("fp16", 11)])
+@pytest.mark.parametrize("storage,bits", [("bf16", 8), ("fp16", 11), ("bf16u", 8)])
 def test_batch_encode_decode_round_trip(storage, bits):
     """Per-tile exponents keep every tile at full 16-bit precision, whatever its level: tiles
     whose values span 1e-30 .. 1e3 decode within half an ulp of the format."""
@@ -147,6 +147,32 @@ def test_batch_encode_decode_round_trip(storage, bits):
                 hi = min(lo + 32, c * N + (x + 1) * syz)
                 m = numpy.abs(want[lo:hi]).max()
                 assert numpy.abs(got[lo:hi] - want[lo:hi]).max() <= m * 2.0 ** (-bits)
+
+
+def test_bf16_without_exponents_matches_bf16_with_them():
+    """Power-of-two tile exponents commute with bfloat16 rounding in the normal range, so the
+    'bf16u' storage (no exponents) steps to the same bits as 'bf16', and its round trip is
+    plain bfloat16 rounding."""
+    from opencl_fdtd_gb300.batch import BatchSimulation
+    kws = [_variant(s, T, 70 + i) for i, (s, T) in enumerate(SHAPES[:3])]
+    a, b = _sims(kws), _sims(kws)
+    src = _sources(a, 15, 9)
+    ba = BatchSimulation(a, storage="bf16", sources=src, steps=15)
+    bb = BatchSimulation(b, storage="bf16u", sources=src, steps=15)
+    ba.run(15)
+    bb.run(15)
+    ba.sync()
+    bb.sync()
+    torch.cuda.synchronize()
+    for x, y in zip(a, b):
+        assert torch.equal(x.E, y.E) and torch.equal(x.H, y.H)
+    vals = (torch.randn(3 * b[0].N, device="cuda") * 10.0 ** torch.empty(3 * b[0].N, device="cuda").uniform_(-20, 3))
+    b[0].E.copy_(vals)
+    bb.load()
+    b[0].E.zero_()
+    bb.sync()
+    torch.cuda.synchronize()
+    assert torch.equal(b[0].E, vals.to(torch.bfloat16).to(torch.float32))
 
 
 def test_batch_rejects_unsupported_simulations():
