@@ -476,20 +476,6 @@ class TeacherData:
         return [int(x.shape[0]) for x in self.X]
 
 
-def sphere_epsilon(shape, n, seed, eps_range=(1.0, 12.0), r_range=(4.0, 24.0), dtype=numpy.float32):
-    """Isotropic eps: vacuum with n seeded dielectric spheres anywhere in the grid."""
-    rng = numpy.random.default_rng(seed)
-    eps = numpy.ones(shape, dtype)
-    x, y, z = (numpy.arange(s, dtype=numpy.float32) for s in shape)
-    for _ in range(int(n)):
-        c = rng.uniform([0, 0, 0], shape)
-        r = rng.uniform(*r_range)
-        e = rng.uniform(*eps_range)
-        d2 = ((x - c[0]) ** 2)[:, None, None] + ((y - c[1]) ** 2)[None, :, None] + ((z - c[2]) ** 2)[None, None, :]
-        eps[d2 < r * r] = e
-    return [eps, eps.copy(), eps.copy()]
-
-
 def dipole_pulse(period: float, polarisation, delay_periods: float = 4.0, width_periods: float = 1.0):
     """Point-dipole waveform per component: sin(2 pi t / P) exp(-((t - t0) / s)^2 / 2) times the
     polarisation's components, s = width_periods * P, t0 = delay_periods * s."""
