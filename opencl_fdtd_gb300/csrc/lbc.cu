@@ -761,14 +761,19 @@ cudaError_t launch_lbc_predict(const LGrid &g, int side, int precision, float me
         k_lbc_predict32<<<gi, T_APPLY, 0, st>>>(g, side, memory, (const float *)W, E, H, pred);
         return cudaGetLastError();
     }
-    static bool attr_set[2] = {false, false};
+    // the shared-memory opt-in is a per-device function attribute: set it once per device
+    // (setting it twice from two threads is harmless)
+    constexpr int MAX_DEV = 64;
+    static bool attr_set[MAX_DEV][2] = {};
     const int split = precision == LBC_BF16X2 ? 1 : 0;
-    cudaError_t e;
-    if (!attr_set[split]) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= MAX_DEV || !attr_set[dev][split]) {
         e = split ? cudaFuncSetAttribute(k_lbc_predict_mma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MMA_SMEM)
                   : cudaFuncSetAttribute(k_lbc_predict_mma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MMA_SMEM);
         if (e != cudaSuccess) return e;
-        attr_set[split] = true;
+        if (dev >= 0 && dev < MAX_DEV) attr_set[dev][split] = true;
     }
     const dim3 gi((maxc + MMA_COLS - 1) / MMA_COLS, (unsigned)g.nface, 1);
     if (split)

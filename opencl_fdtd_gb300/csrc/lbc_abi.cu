@@ -175,6 +175,7 @@ int fdtd_lbc_predict(const int32_t shape[3], int32_t face_mask, int32_t side, in
     if (rc) return rc;
     if (!E || !H || !pred) return bad("fdtd_lbc_predict: NULL pointer");
     if (side < -1 || side > 1) return bad("fdtd_lbc_predict: side must be -1, 0 or 1");
+    if (!(memory >= 0.f && memory < 1.f)) return bad("fdtd_lbc_predict: memory must be in [0, 1)");
     const LGrid g = grid_of(shape, face_mask);
     if (pred_floats < (int64_t)g.ncol * LBC_OUT) return bad("fdtd_lbc_predict: pred too small");
     return check_cuda(launch_lbc_predict(g, side, precision, memory, weights, E, H, pred, (cudaStream_t)stream),
@@ -211,6 +212,7 @@ int fdtd_lbc_attach(FdtdPlan *plan, int32_t face_mask, int32_t precision, float 
     int rc = check_weights(precision, weights, "fdtd_lbc_attach");
     if (rc) return rc;
     if (!pred) return bad("fdtd_lbc_attach: pred is NULL");
+    if (!(memory >= 0.f && memory < 1.f)) return bad("fdtd_lbc_attach: memory must be in [0, 1)");
     const int32_t shape[3] = {(int32_t)plan->sx, (int32_t)plan->sy, (int32_t)plan->sz};
     if (!shape_ok(shape)) return bad("fdtd_lbc_attach: every extent must be >= 2");
     const LGrid g = grid_of(shape, face_mask);
