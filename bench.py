@@ -744,7 +744,8 @@ def run_c5(args):
     pick = min(pool, key=lambda k: verdicts[k]["reflection_db"])
     net = cands[pick][0]
     verdict = verdicts[pick]
-    lb = L.LearnedBoundary(net, "bf16x2")
+    lin_ok = all(a is not None for a in net.linear)
+    lb = L.LearnedBoundary(net, "linear" if lin_ok else "bf16x2")
     zero = L.BoundaryNet(seed=3, memory=L.MUR_MEMORY)
     zero.params.zero_()
     held = L.reflection_db(L.LearnedBoundary(zero, "bf16x2"), shape=(96, 96, 96), steps=400, period=20.0)
@@ -834,14 +835,41 @@ def run_c5(args):
     tc_peak = float(peaks.get("bf16_tflops", 1900.0))
     lb.detach(thin)
     thin.close()
+    del thin
 
-    deployed = "learned" if verdict["accepted"] else "cpml"
+    # the learned layer on the z faces only (air above and below the slab), CPML on x and y
+    # where the slab crosses, with the linear-layer kernel when the picked network is linear
+    zprec = "linear" if lin_ok else "bf16x2"
+    lbz = L.LearnedBoundary(net, zprec, faces=["-z", "+z"])
+    verdict_z = L.judge(lbz)
+    zshape = (shape[0], shape[1], shape[2] - 2 * thin_off)
+    kw_z = dict(kw)
+    kw_z["epsilon"] = [numpy.ascontiguousarray(e[:, :, thin_off:thin_off + zshape[2]]) for e in kw["epsilon"]]
+    kw_z["pmls"] = [p_ for p_ in kw["pmls"] if p_["axis"] != "z"]
+    kw_z["dt"] = L.DEFAULT_DT
+    thz = Simulation(**kw_z)
+    lbz.attach(thz)
+    ind_z = comp * thz.N + int(numpy.ravel_multi_index((c[0], c[1], c[2] - thin_off), zshape))
+    ms_z = timed(thz, ind_z)
+    Ez = thz.E.view(3, *zshape)[:, 8:8 + useful[0], 8:8 + useful[1], 2:2 + useful[2]]
+    fin_z = bool(torch.isfinite(Ez).all())
+    l2_z = float(torch.linalg.norm((Ez - Ep).double()) / torch.linalg.norm(Ep.double())) if fin_z else float("inf")
+    lbz.detach(thz)
+    thz.close()
+    del thz
+    v_z = useful_cells * K / (ms_z * 1e-3) / 1e6
+
     v_plain = useful_cells * K / (ms_plain * 1e-3) / 1e6
     v_thin = useful_cells * K / (ms_thin * 1e-3) / 1e6
-    value = v_thin if deployed == "learned" else v_plain
+    if verdict["accepted"]:
+        deployed, value, ms_dep = "learned", v_thin, ms_thin
+    elif verdict_z["accepted"]:
+        deployed, value, ms_dep = "learned on z faces, CPML on x and y", v_z, ms_z
+    else:
+        deployed, value, ms_dep = "cpml", v_plain, ms_plain
     line = {
         "metric": METRIC + " (useful interior)", "value": round(value, 2), "unit": UNIT, "n_gpus": 1, "steps": K,
-        "warmup": 3, "ms_per_step": round((ms_thin if deployed == "learned" else ms_plain) / K, 5),
+        "warmup": 3, "ms_per_step": round(ms_dep / K, 5),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 fields; boundary MLP bf16 weights, f32 accumulation (bf16x2 activations)",
         "data": "synthetic (seeded)",
@@ -865,10 +893,18 @@ def run_c5(args):
         "judge_seconds": round(judge_s, 1),
         "plain_cpml8": {"ms": round(ms_plain, 3), "useful_mcells_per_s": round(v_plain, 2),
                         "grid": list(shape)},
-        "thin_learned": {"ms": round(ms_thin, 3), "useful_mcells_per_s": round(v_thin, 2), "grid": list(thin_shape),
+        "thin_learned": {"precision": "linear" if lin_ok else "bf16x2",
+                         "ms": round(ms_thin, 3), "useful_mcells_per_s": round(v_thin, 2), "grid": list(thin_shape),
                          "finite_after_steps": finite,
                          "interior_rel_l2_vs_plain_cpml8": l2 if math.isfinite(l2) else "inf",
                          "predict_ms_per_step": round(ms_pred, 4), "boundary_columns": n_cols},
+        "thin_z_learned": {"faces": "learned on z (air), 8-cell CPML on x and y", "precision": zprec,
+                           "ms": round(ms_z, 3), "useful_mcells_per_s": round(v_z, 2), "grid": list(zshape),
+                           "vs_plain": round(v_z / v_plain, 3), "finite_after_steps": fin_z,
+                           "interior_rel_l2_vs_plain_cpml8": l2_z if math.isfinite(l2_z) else "inf",
+                           "verdict": {k: (round(v, 2) if isinstance(v, float) and math.isfinite(v) else
+                                           ({str(a): round(b, 2) for a, b in v.items()} if isinstance(v, dict) else v))
+                                       for k, v in verdict_z.items()}},
         "roofline": {"bound": "tensor", "achieved": round(flops / (ms_pred * 1e-3) / 1e12, 2),
                      "peak": tc_peak, "unit": "TFLOP/s", "frac": round(flops / (ms_pred * 1e-3) / 1e12 / tc_peak, 4),
                      "traffic": None, "kernel": "k_lbc_predict_mma<split> (bf16 mma.sync, algorithmic FLOPs "

@@ -318,6 +318,8 @@ int fdtd_batch_decode(FdtdBatch *batch, int32_t v, int32_t field, float *dst, vo
 #define FDTD_LBC_F32 0              /* float32 weights, CUDA cores */
 #define FDTD_LBC_BF16 1             /* bfloat16 weights and activations, tensor cores */
 #define FDTD_LBC_BF16X2 2           /* bfloat16 weights, activations as two bfloat16 parts */
+#define FDTD_LBC_LINEAR 3           /* an exactly linear layer: float32 [6][109][6], rows = the
+                                       108 inputs then the bias; ghost = A^T stencil + r bias */
 
 /* Columns of the faces in face_mask (whole planes); face_offsets[f] (f = 2 * axis + side) is
  * the first column of face f (-1 when absent), face_offsets[6] the total. face_offsets may be
@@ -352,7 +354,8 @@ int fdtd_adam(float *params, const float *grad, float *m, float *v, int32_t n, f
 int fdtd_lbc_pack(const float *params, void *packed, void *stream);
 /* Ghost values [ncol][6] of the faces of side `side` (-1: all): pred = r * (network output)
  * + memory * pred, pred holding the previous step's ghosts (zero before the first step);
- * weights: float32 parameters (FDTD_LBC_F32) or the packed layout (BF16, BF16X2). memory =
+ * weights: float32 parameters (FDTD_LBC_F32), the packed layout (BF16, BF16X2) or the linear
+ * map of a layer that is exactly linear (FDTD_LBC_LINEAR). memory =
  * (1 - c dt) / (1 + c dt) makes room for Mur's first-order condition (its other terms are
  * linear in the stencil); memory = 0: ghosts from the current stencil alone. */
 int fdtd_lbc_predict(const int32_t shape[3], int32_t face_mask, int32_t side, int32_t precision, float memory,

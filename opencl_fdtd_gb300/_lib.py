@@ -149,6 +149,7 @@ FDTD_LBC_FIX_H = 2
 FDTD_LBC_F32 = 0
 FDTD_LBC_BF16 = 1
 FDTD_LBC_BF16X2 = 2
+FDTD_LBC_LINEAR = 3
 
 _LIB = None
 _LOCK = threading.Lock()

@@ -332,6 +332,46 @@ __global__ void __launch_bounds__(T_APPLY) k_lbc_predict32(const LGrid g, int si
     }
 }
 
+// an exactly linear layer (LBC_LINEAR): one thread per column, 108 x 6 products, weights
+// [6][IN + 1][OUT] float32 in shared memory
+__global__ void __launch_bounds__(T_APPLY) k_lbc_predict_lin(const LGrid g, int side, float memory, const float *W,
+                                                             const float *E, const float *H, float *pred)
+{
+    __shared__ float w[(LBC_IN + 1) * LBC_OUT];
+    const LFace &f = g.face[blockIdx.y];
+    if (side >= 0 && f.side != side) return;                 // block-uniform
+    const float *Wf = W + (uint64_t)(f.axis * 2 + f.side) * (LBC_IN + 1) * LBC_OUT;
+    for (int i = threadIdx.x; i < (LBC_IN + 1) * LBC_OUT; i += blockDim.x) w[i] = Wf[i];
+    __syncthreads();
+    const uint32_t c = blockIdx.x * T_APPLY + threadIdx.x;
+    if (c >= f.ncol) return;
+    const uint32_t u = f.u0 + c / f.nv, v = f.v0 + c % f.nv;
+    float acc[LBC_OUT];
+#pragma unroll
+    for (int o = 0; o < LBC_OUT; ++o) acc[o] = 0.f;
+    float ss = 0.f;
+#pragma unroll
+    for (int d = 0; d < 2; ++d)
+#pragma unroll
+        for (int du = -1; du <= 1; ++du)
+#pragma unroll
+            for (int dv = -1; dv <= 1; ++dv) {
+                const uint64_t i = cell_of(g, f, u, v, d, du, dv);
+                const int k0 = ((d * 3 + (du + 1)) * 3 + (dv + 1)) * 6;
+#pragma unroll
+                for (int q = 0; q < 6; ++q) {
+                    const float xv = q < 3 ? E[q * g.N + i] : H[(q - 3) * g.N + i];
+                    ss += xv * xv;
+#pragma unroll
+                    for (int o = 0; o < LBC_OUT; ++o) acc[o] += xv * w[(k0 + q) * LBC_OUT + o];
+                }
+            }
+    const float r = sqrtf(ss * (1.0f / LBC_IN));
+    float *out = pred + (uint64_t)(f.col0 + c) * LBC_OUT;
+#pragma unroll
+    for (int o = 0; o < LBC_OUT; ++o) out[o] = acc[o] + r * w[LBC_IN * LBC_OUT + o] + memory * out[o];
+}
+
 // ---- bfloat16 tensor-core inference (mma.sync m16n8k16, float32 accumulation) ------------------
 // Weights are packed once per face into the B-fragment order of mma.m16n8k16 (PTX ISA, "Matrix
 // fragments for mma.m16n8k16"): for k-step ks and n-tile nt, lane (g = lane / 4, t = lane % 4)
@@ -756,9 +796,10 @@ cudaError_t launch_lbc_predict(const LGrid &g, int side, int precision, float me
     if (!g.ncol) return cudaSuccess;
     uint32_t maxc = 0;
     for (int f = 0; f < g.nface; ++f) maxc = g.face[f].ncol > maxc ? g.face[f].ncol : maxc;
-    if (precision == LBC_F32) {
+    if (precision == LBC_F32 || precision == LBC_LINEAR) {
         const dim3 gi((maxc + T_APPLY - 1) / T_APPLY, (unsigned)g.nface, 1);
-        k_lbc_predict32<<<gi, T_APPLY, 0, st>>>(g, side, memory, (const float *)W, E, H, pred);
+        if (precision == LBC_F32) k_lbc_predict32<<<gi, T_APPLY, 0, st>>>(g, side, memory, (const float *)W, E, H, pred);
+        else k_lbc_predict_lin<<<gi, T_APPLY, 0, st>>>(g, side, memory, (const float *)W, E, H, pred);
         return cudaGetLastError();
     }
     // the shared-memory opt-in is a per-device function attribute: set it once per device

@@ -29,6 +29,9 @@ constexpr int LBC_PACK_WORDS = 7 * 8 * 64 + 4 * 8 * 64 + 4 * 64 + 64 + 64 + 8;  
 constexpr int LBC_F32 = 0;
 constexpr int LBC_BF16 = 1;
 constexpr int LBC_BF16X2 = 2;
+// an exactly linear layer, float32 [6 faces][LBC_IN + 1][LBC_OUT] (rows: inputs, then the bias):
+// ghost = sum_k A[k][o] stencil_k + r A[IN][o] (the normalisation cancels)
+constexpr int LBC_LINEAR = 3;
 
 // one face of a grid as the boundary kernels see it
 struct LFace {

@@ -11,7 +11,8 @@ using namespace fdtd;
 static_assert(FDTD_LBC_IN == LBC_IN && FDTD_LBC_HID == LBC_HID && FDTD_LBC_OUT == LBC_OUT, "stencil sizes");
 static_assert(FDTD_LBC_NPARAM == LBC_NPARAM && FDTD_LBC_PACK_WORDS == LBC_PACK_WORDS, "parameter layout");
 static_assert(FDTD_LBC_FIX_E == LBC_FIX_E && FDTD_LBC_FIX_H == LBC_FIX_H, "fix-up fields");
-static_assert(FDTD_LBC_F32 == LBC_F32 && FDTD_LBC_BF16 == LBC_BF16 && FDTD_LBC_BF16X2 == LBC_BF16X2, "precision");
+static_assert(FDTD_LBC_F32 == LBC_F32 && FDTD_LBC_BF16 == LBC_BF16 && FDTD_LBC_BF16X2 == LBC_BF16X2 &&
+                  FDTD_LBC_LINEAR == LBC_LINEAR, "precision");
 
 namespace {
 
@@ -157,10 +158,11 @@ int fdtd_lbc_pack(const float *params, void *packed, void *stream)
 
 static int check_weights(int32_t precision, const void *weights, const char *what)
 {
-    if (precision != FDTD_LBC_F32 && precision != FDTD_LBC_BF16 && precision != FDTD_LBC_BF16X2)
+    if (precision != FDTD_LBC_F32 && precision != FDTD_LBC_BF16 && precision != FDTD_LBC_BF16X2 &&
+        precision != FDTD_LBC_LINEAR)
         return bad((std::string(what) + ": unknown precision").c_str());
     if (!weights) return bad((std::string(what) + ": weights is NULL").c_str());
-    if (precision != FDTD_LBC_F32 && (uintptr_t)weights % 16)
+    if ((precision == FDTD_LBC_BF16 || precision == FDTD_LBC_BF16X2) && (uintptr_t)weights % 16)
         return bad((std::string(what) + ": packed weights must be 16-byte aligned").c_str());
     return FDTD_OK;
 }

@@ -62,7 +62,8 @@ import numpy
 from . import _lib
 
 FACES_ALL = 63
-PRECISIONS = {"f32": _lib.FDTD_LBC_F32, "bf16": _lib.FDTD_LBC_BF16, "bf16x2": _lib.FDTD_LBC_BF16X2}
+PRECISIONS = {"f32": _lib.FDTD_LBC_F32, "bf16": _lib.FDTD_LBC_BF16, "bf16x2": _lib.FDTD_LBC_BF16X2,
+              "linear": _lib.FDTD_LBC_LINEAR}
 NPARAM = _lib.FDTD_LBC_NPARAM
 IN, HID, OUT = _lib.FDTD_LBC_IN, _lib.FDTD_LBC_HID, _lib.FDTD_LBC_OUT
 # offsets in the parameter vector (W1 b1 W2 b2 W3 b3, row-major [in][out])
@@ -205,6 +206,10 @@ class BoundaryNet:
         self._bufs = {}
         self._wout = {}
         self.history = {}
+        # the linear map of each face whose network is an exactly embedded linear map (None
+        # once Adam has changed the parameters)
+        self.linear = [None] * 6
+        self._linear_dev = None
 
     # ---- kernels ---------------------------------------------------------------------------
     def _buffers(self, B):
@@ -263,6 +268,8 @@ class BoundaryNet:
 
     def adam_step(self, face: int, grad, lr: float, betas=(0.9, 0.999), eps: float = 1e-8):
         self.steps[face] += 1
+        self.linear[face] = None
+        self._linear_dev = None
         _lib.check(_lib.load().fdtd_adam(self.params[face].data_ptr(), grad.data_ptr(), self.m[face].data_ptr(),
                                          self.v[face].data_ptr(), NPARAM, float(lr), float(betas[0]),
                                          float(betas[1]), float(eps), self.steps[face], self._stream()))
@@ -341,6 +348,8 @@ class BoundaryNet:
         self.v[face].zero_()
         self.steps[face] = 0
         self._packed = None
+        self.linear[face] = numpy.array(A, dtype=numpy.float64)
+        self._linear_dev = None
 
     def fit_linear(self, data: "TeacherData", ridge: float = 1e-2, faces=range(6), prior: str = None,
                    support: str = None):
@@ -403,10 +412,18 @@ class BoundaryNet:
 
     # ---- inference weights -----------------------------------------------------------------
     def weights(self, precision: str = "bf16"):
-        """Device weights for fdtd_lbc_predict / attach in ``precision``."""
+        """Device weights for fdtd_lbc_predict / attach in ``precision`` ('linear': the linear
+        maps of a network that is an exactly embedded linear map on every face)."""
         torch = _torch()
         if precision == "f32":
             return self.params
+        if precision == "linear":
+            if any(a is None for a in self.linear):
+                raise ValueError("'linear' inference needs a linear map on every face (embed_linear / fit_linear, "
+                                 "no Adam step since)")
+            if self._linear_dev is None:
+                self._linear_dev = torch.from_numpy(numpy.stack(self.linear).astype(numpy.float32)).to(self.device)
+            return self._linear_dev
         if self._packed is None:
             packed = torch.empty((6, _lib.FDTD_LBC_PACK_WORDS), dtype=torch.int32, device=self.device)
             _lib.check(_lib.load().fdtd_lbc_pack(self.params.data_ptr(), packed.data_ptr(), self._stream()))
@@ -414,7 +431,10 @@ class BoundaryNet:
         return self._packed
 
     def state_dict(self) -> dict:
-        return {"params": self.params.detach().cpu().numpy(), "dt": self.dt, "memory": self.memory}
+        st = {"params": self.params.detach().cpu().numpy(), "dt": self.dt, "memory": self.memory}
+        if all(a is not None for a in self.linear):
+            st["linear"] = numpy.stack(self.linear)
+        return st
 
     def load_state_dict(self, st: dict):
         torch = _torch()
@@ -422,17 +442,23 @@ class BoundaryNet:
         self.dt = float(st.get("dt", self.dt))
         self.memory = float(st.get("memory", self.memory))
         self._packed = None
+        lin = st.get("linear")
+        self.linear = [None] * 6 if lin is None else [numpy.asarray(a, numpy.float64) for a in lin]
+        self._linear_dev = None
 
     def save(self, path):
         st = self.state_dict()
-        numpy.savez(path, params=st["params"], dt=numpy.float64(st["dt"]), memory=numpy.float64(st["memory"]))
+        extra = {"linear": st["linear"]} if "linear" in st else {}
+        numpy.savez(path, params=st["params"], dt=numpy.float64(st["dt"]), memory=numpy.float64(st["memory"]),
+                    **extra)
 
     @classmethod
     def load(cls, path, device=None):
         z = numpy.load(path)
         memory = float(z["memory"]) if "memory" in z.files else 0.0
         net = cls(device=device, dt=float(z["dt"]), memory=memory)
-        net.load_state_dict({"params": z["params"], "dt": float(z["dt"]), "memory": memory})
+        net.load_state_dict({"params": z["params"], "dt": float(z["dt"]), "memory": memory,
+                             "linear": z["linear"] if "linear" in z.files else None})
         return net
 
 

@@ -422,6 +422,29 @@ def test_learned_map_on_murs_stencil_is_stable_and_fits_better_than_mur(mur_trai
     assert first < held - 10.0, (first, held)
 
 
+def test_linear_inference_matches_the_network(mur_training):
+    """A network that is an exactly embedded linear map gives the same ghosts through the
+    'linear' kernel as through the float32 MLP kernel (GELU kept in its linear range)."""
+    L, data, net, mur = mur_training
+    shape = (14, 11, 9)
+    E, H = _fields(shape, 50, 0.05)
+    Ed, Hd = _cuda(E), _cuda(H)
+    n, _ = L.columns(shape)
+    prev = numpy.random.default_rng(51).standard_normal((n, 6)).astype(numpy.float32) * 0.01
+    w = numpy.concatenate([net.output_weights(f).cpu().numpy()[None, :].repeat(1, 0) for f in range(6)])
+    p32 = _predict(L, shape, 63, "f32", net.params, Ed, Hd, memory=net.memory, prev=prev)
+    plin = _predict(L, shape, 63, "linear", net.weights("linear"), Ed, Hd, memory=net.memory, prev=prev)
+    _, face_of = O.column_cells(shape, 63)
+    used = w[face_of] > 0
+    scale = numpy.max(numpy.abs(p32[used]))
+    assert numpy.max(numpy.abs(p32[used] - plin[used])) <= 1e-4 * scale
+    # an Adam step leaves no linear map behind
+    net2 = L.BoundaryNet(seed=4, memory=L.MUR_MEMORY)
+    net2.embed_linear(0, L.mur_map(0))
+    with pytest.raises(ValueError):
+        net2.weights("linear")
+
+
 def test_judge_and_fallback(small_training):
     """The judge's verdict decides between the learned layer and CPML."""
     L, data, net, before, start, after = small_training
