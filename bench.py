@@ -699,10 +699,10 @@ def run_c5(args):
     """Learned thin boundary on the c2 cavity: teacher data (Mur-memory targets), candidate
     networks (least squares on Mur's stencil, least squares shrunk towards Mur's map at two
     strengths, and Mur's map itself),
-    the judge on each (reflection against a doubled grid, long-run stability), then the c2
+    the evaluation of each (reflection against a doubled grid, long-run stability), then the c2
     cavity timed (a) plain with its 8-cell CPML (395x345x73) and (b) cut to its useful
     interior plus a 2-cell learned layer per face (383x333x61) with the picked candidate; the
-    line reports the form the judge deploys. Throughput counts useful-interior cells
+    line reports the form the evaluation deploys. Throughput counts useful-interior cells
     (379x329x57 in both forms)."""
     import torch
     from opencl_fdtd_gb300 import Simulation, workloads
@@ -716,7 +716,7 @@ def run_c5(args):
     tvar = {f: float(((data.T[f] ** 2) * probe.output_weights(f)).mean()) for f in range(6)}
     samples = data.sizes()
     # candidates: least squares shrunk towards Mur's map (two strengths), and Mur's map itself;
-    # the judge (bf16x2 inference, the deployed precision) picks the best accepted one
+    # the evaluation (bf16x2 inference, the deployed precision) picks the best accepted one
     cands = {}
     t0 = time.perf_counter()
     for name, rho, support in (("learned, Mur stencil", 0.0, "mur"), ("learned, shrink 0.3", 0.3, None),
@@ -734,8 +734,8 @@ def run_c5(args):
     del data
     torch.cuda.empty_cache()
     t0 = time.perf_counter()
-    verdicts = {name: L.judge(L.LearnedBoundary(n_, "bf16x2")) for name, (n_, _) in cands.items()}
-    judge_s = time.perf_counter() - t0
+    verdicts = {name: L.evaluate(L.LearnedBoundary(n_, "bf16x2")) for name, (n_, _) in cands.items()}
+    evaluate_s = time.perf_counter() - t0
     # the deployed candidate: the best accepted one; for the timing of the thin form when none
     # is accepted, the best stable learned one
     accepted = [k for k, v in verdicts.items() if v["accepted"]]
@@ -841,7 +841,7 @@ def run_c5(args):
     # where the slab crosses, with the linear-layer kernel when the picked network is linear
     zprec = "linear" if lin_ok else "bf16x2"
     lbz = L.LearnedBoundary(net, zprec, faces=["-z", "+z"])
-    verdict_z = L.judge(lbz)
+    verdict_z = L.evaluate(lbz)
     zshape = (shape[0], shape[1], shape[2] - 2 * thin_off)
     kw_z = dict(kw)
     kw_z["epsilon"] = [numpy.ascontiguousarray(e[:, :, thin_off:thin_off + zshape[2]]) for e in kw["epsilon"]]
@@ -890,7 +890,7 @@ def run_c5(args):
         "training": {"data_seconds": round(data_s, 1), "fit_seconds": round(train_s, 1),
                      "samples_per_face": samples, "memory": round(L.MUR_MEMORY, 5),
                      "relative_loss_per_face": rel},
-        "judge_seconds": round(judge_s, 1),
+        "evaluate_seconds": round(evaluate_s, 1),
         "plain_cpml8": {"ms": round(ms_plain, 3), "useful_mcells_per_s": round(v_plain, 2),
                         "grid": list(shape)},
         "thin_learned": {"precision": "linear" if lin_ok else "bf16x2",

@@ -31,7 +31,7 @@ through fdtd_mlp_forward / fdtd_mlp_backward / fdtd_adam. Inference uses bfloat1
 the tensor cores with float32 accumulation (``precision='bf16'``; 'bf16x2' also splits the
 activations into two bfloat16 parts; 'f32' runs float32 weights on the CUDA cores).
 
-Judge and fallback (``reflection_db``, ``judge``, ``thin_or_cpml``): a run with the learned
+Evaluation and fallback (``reflection_db``, ``evaluate``, ``thin_or_cpml``): a run with the learned
 boundary is compared with a plain CPML run of a grid twice as large in every learned
 direction; the reflection is the largest error seen in the shell of cells next to the learned
 faces relative to the largest field that reached that shell, and a long run checks that the
@@ -47,7 +47,7 @@ about 10% RMS and, over the first pass of a pulse, leave an error some 30 dB bel
 2-cell layer without the network (zero ghosts), but in closed-loop feedback they grow after
 250-500 steps; fitted on Mur's stencil only (``fit_linear(support='mur')``) the layer is
 stable and beats Mur's own coefficients (-22 against -18 dB in the training band). None
-reaches -40 dB, so the judge rejects them and the simulation falls back to CPML.
+reaches -40 dB, so the evaluation rejects them and the simulation falls back to CPML.
 
 opencl_fdtd has no counterpart of this module: it absorbs with CPML only
 (opencl_fdtd/simulation.py:274-319).
@@ -840,7 +840,7 @@ def reflection_db(boundary: LearnedBoundary, shape=(64, 64, 64), steps: int = 40
             "shape": tuple(shape), "big_shape": big_shape}
 
 
-def judge(boundary: LearnedBoundary, shape=(96, 96, 96), steps: int = 400, periods=(20.0, 68.0),
+def evaluate(boundary: LearnedBoundary, shape=(96, 96, 96), steps: int = 400, periods=(20.0, 68.0),
           stability_shape=(64, 64, 64), stability_steps: int = 3000, threshold_db: float = -40.0,
           growth_db: float = 0.0):
     """The boundary's verdict: the worst reflection (``reflection_db`` over ``steps`` steps, one
@@ -863,18 +863,18 @@ def judge(boundary: LearnedBoundary, shape=(96, 96, 96), steps: int = 400, perio
             "accepted": bool(stable and math.isfinite(worst) and worst <= threshold_db)}
 
 
-def thin_or_cpml(kwargs: dict, boundary: LearnedBoundary, judged_db: float = None, threshold_db: float = -40.0,
+def thin_or_cpml(kwargs: dict, boundary: LearnedBoundary, reflection_db_value: float = None, threshold_db: float = -40.0,
                  cpml_thickness: int = 8, verdict: dict = None):
     """A Simulation for ``kwargs`` (constructor arguments without CPML on the boundary's faces):
-    with the learned boundary attached when it passed (``verdict['accepted']`` from ``judge``,
-    or ``judged_db`` at most ``threshold_db`` when no verdict is given), else with a
+    with the learned boundary attached when it passed (``verdict['accepted']`` from ``evaluate``,
+    or ``reflection_db_value`` at most ``threshold_db`` when no verdict is given), else with a
     ``cpml_thickness``-cell CPML on those faces instead. Returns (sim, 'learned' | 'cpml')."""
     from .simulation import Simulation
     kw = dict(kwargs)
     if verdict is not None:
         ok = bool(verdict.get("accepted"))
     else:
-        ok = judged_db is not None and math.isfinite(judged_db) and judged_db <= threshold_db
+        ok = reflection_db_value is not None and math.isfinite(reflection_db_value) and reflection_db_value <= threshold_db
     if ok:
         sim = Simulation(**kw)
         boundary.attach(sim)

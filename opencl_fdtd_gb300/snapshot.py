@@ -3,9 +3,9 @@ Field snapshots and checkpoints.
 
 save_snapshot writes what opencl_fdtd's example driver saves at the end of a run
 (fdtd.py:181-191): a dict {'grid', 'E', 'H'[, 'S']} whose fields are unvec'd to
-[f_x, f_y, f_z] arrays of the grid shape, pickled and lzma-compressed. The driver pickles
-with dill, which reads plain pickles; 'grid' is whatever the caller passes (the driver's
-gridlock.Grid) or a dict describing the grid.
+[f_x, f_y, f_z] arrays of the grid shape, pickled and lzma-compressed. The example script
+pickles with dill, which reads plain pickles; 'grid' is whatever the caller passes (the
+script's gridlock.Grid) or a dict describing the grid.
 
 save_checkpoint / load_checkpoint keep everything needed to resume a run bit for bit
 (fields, CPML auxiliary arrays, step counter; Simulation.state_dict).

@@ -4,7 +4,7 @@ Harness for the C restatement of the reference kernels (TEST INFRASTRUCTURE).
 ``PortSimulation`` mirrors the reference's ``Simulation`` (opencl_fdtd/simulation.py:77-271)
 on host numpy arrays and drives oracle/fdtd_port.c through ctypes. It is the checker the CUDA
 path is compared with, the FP64 oracle (``float_type=numpy.float64``) for error reports, and
-the judge for the two extensions the reference lacks (diagonal mu, Bloch-phase coupling).
+the checker for the two extensions the reference lacks (diagonal mu, Bloch-phase coupling).
 
 PML psi arrays keep the reference's layout (opencl_fdtd/kernels/update_e.cl:92):
 shape (T, s_u, s_v) for a face on axis r with (u, v) the other two axes in xyz order.

@@ -153,7 +153,7 @@ def call_kernel(lib, args_decl, values, nthreads: int = 0):
 # fake pyopencl / fdfd_tools
 # --------------------------------------------------------------------------------------------
 class FakeArray(numpy.ndarray):
-    """Stand-in for pyopencl.array.Array: host memory with the ``get()`` the driver uses."""
+    """Stand-in for pyopencl.array.Array: host memory with the ``get()`` the example script (fdtd.py) uses."""
 
     def get(self):
         return numpy.array(self)

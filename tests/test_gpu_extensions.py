@@ -1,5 +1,5 @@
 """GPU parity for what the reference lacks: diagonal anisotropic mu and Bloch-phase coupling of
-split complex fields (both judged by the oracle's restatement, bit for bit in float32 and
+split complex fields (both checked against the oracle's restatement, bit for bit in float32 and
 float64), a Bloch-theorem check that needs no oracle, and the dt/eps cache refresh."""
 import copy
 import math

@@ -445,11 +445,11 @@ def test_linear_inference_matches_the_network(mur_training):
         net2.weights("linear")
 
 
-def test_judge_and_fallback(small_training):
-    """The judge's verdict decides between the learned layer and CPML."""
+def test_evaluation_and_fallback(small_training):
+    """The evaluation's verdict decides between the learned layer and CPML."""
     L, data, net, before, start, after = small_training
     lb = L.LearnedBoundary(net, "bf16x2")
-    v = L.judge(lb, shape=(24, 24, 24), steps=60, periods=(14.0,), stability_shape=(24, 24, 24),
+    v = L.evaluate(lb, shape=(24, 24, 24), steps=60, periods=(14.0,), stability_shape=(24, 24, 24),
                 stability_steps=200)
     assert set(v) >= {"reflection_db", "stable", "accepted", "growth_onset_step"}
     kw = dict(epsilon=[numpy.ones((12, 12, 12), numpy.float32)] * 3, pmls=[], do_poynting=False,
@@ -458,5 +458,5 @@ def test_judge_and_fallback(small_training):
     assert used == ("learned" if v["accepted"] else "cpml")
     sim, used = L.thin_or_cpml(kw, lb, verdict={"accepted": False})
     assert used == "cpml" and len(sim.pmls) == 6
-    sim, used = L.thin_or_cpml(kw, lb, judged_db=-45.0)
+    sim, used = L.thin_or_cpml(kw, lb, reflection_db_value=-45.0)
     assert used == "learned" and sim.pmls == []

@@ -1,5 +1,5 @@
-"""The snapshot layout helpers (no GPU needed): unvec/vec round trip and the driver's
-{'grid', 'E', 'H', 'S'} file format."""
+"""The snapshot layout helpers (no GPU needed): unvec/vec round trip and the example
+script's (fdtd.py) {'grid', 'E', 'H', 'S'} file format."""
 import lzma
 import pickle
 
