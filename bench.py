@@ -695,6 +695,63 @@ def run_c4(args):
     print(json.dumps(line), flush=True)
 
 
+def run_c3(args):
+    """Anisotropic + Bloch cell (128x128x256, split complex float32, Bloch phases on x and y,
+    8-cell CPML on z, diagonal eps / mu spheres with one PEC sphere): Simulation.run over the
+    per-update kernels (E, F, H, G per step), timed with CUDA events; fields start from seeded
+    random values (the plane-wave source does not change the work). Algorithmic bytes per
+    cell-step: the real and imaginary passes each read and write their field once and read the
+    coupled partners and eps / mu; the count is spelled out below."""
+    import torch
+    from opencl_fdtd_gb300 import Simulation, workloads
+    torch.cuda.set_device(0)
+    wl = workloads.get("c3")
+    kw = dict(wl["kwargs"])
+    shape = wl["shape"]
+    N = int(numpy.prod(shape))
+    rng = numpy.random.default_rng(33)
+    kw["initial_fields"] = {k: [(1e-3 * rng.standard_normal(shape)).astype(numpy.float32) for _ in range(3)]
+                            for k in ("E", "H", "F", "G")}
+    sim = Simulation(**kw)
+    K = args.steps if args.steps != 8000 else 2000
+    W = max(args.warmup if args.warmup != 50 else 20, 3)
+    sim.run(W)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(sim.queue)
+    sim.run(K)
+    e1.record(sim.queue)
+    e1.synchronize()
+    clock = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    finite = bool(torch.isfinite(sim.E).all())
+    # bytes per cell-step, one access per array per pass (float32): the E pass reads and writes
+    # E and reads H and eps, the F pass likewise F, G and eps, the H and G passes their field,
+    # the E-type field and mu (the Bloch partner is read only on the wrapped planes): 4 passes x
+    # 4 arrays x 3 components x 4 B = 192 B per cell; CPML psi on the z faces: 4 passes x
+    # 2 arrays read and written x 4 B = 64 B per face-cell
+    fc = workloads.face_cells(shape, kw["pmls"])
+    step_bytes = 192.0 * N + 64.0 * fc
+    peak, peak_kind = peak_hbm()
+    gbs = step_bytes * K / (ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(N * K / (ms * 1e-3) / 1e6, 2), "unit": UNIT, "n_gpus": 1,
+        "steps": K, "warmup": W, "ms_per_step": round(ms / K, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (split complex)", "data": "synthetic (seeded spheres, random fields)",
+        "config": {"workload": "c3: " + wl["describe"], "cells": N, "cpml_face_cells": fc,
+                   "path": "Simulation.run, per-update kernels (E, F, H, G)",
+                   "l2": "fields (%.0f MB) larger than the 129 MB L2; no flush" % (N * 4 * 3 * 6 / 1e6)},
+        "step_roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+                          "frac": round(gbs / peak, 4), "bytes_per_step": step_bytes, "peak_kind": peak_kind},
+        "finite_after_steps": finite, "clocks": clock,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_c5(args):
     """Learned thin boundary on the c2 cavity: teacher data (Mur-memory targets), candidate
     networks (least squares on Mur's stencil, least squares shrunk towards Mur's map at two
@@ -920,5 +977,7 @@ if __name__ == "__main__":
         run_c4(_a)
     elif _a.workload == "c5" and _a.impl == "ours":
         run_c5(_a)
+    elif _a.workload == "c3" and _a.impl == "ours":
+        run_c3(_a)
     else:
         main()
