@@ -898,7 +898,7 @@ def run_c5(args):
     # where the slab crosses, with the linear-layer kernel when the picked network is linear
     zprec = "linear" if lin_ok else "bf16x2"
     lbz = L.LearnedBoundary(net, zprec, faces=["-z", "+z"])
-    verdict_z = L.evaluate(lbz)
+    verdict_z = L.evaluate(lbz, cpml_other=8)
     zshape = (shape[0], shape[1], shape[2] - 2 * thin_off)
     kw_z = dict(kw)
     kw_z["epsilon"] = [numpy.ascontiguousarray(e[:, :, thin_off:thin_off + zshape[2]]) for e in kw["epsilon"]]

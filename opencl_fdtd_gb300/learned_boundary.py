@@ -763,7 +763,7 @@ class LearnedBoundary:
 
 def reflection_db(boundary: LearnedBoundary, shape=(64, 64, 64), steps: int = 400, every: int = 10,
                   period: float = 20.0, polarisation=(0.3, 1.0, 0.2), epsilon=None, cpml: int = 16,
-                  source=None, shell: int = 8):
+                  source=None, shell: int = 8, cpml_other: int = 0):
     """Reflection of a boundary in dB: the same dipole pulse in (a) ``shape`` with the boundary
     on the faces of its mask and (b) a plain run on a grid twice as large in every learned
     direction (``shape`` centred) with a ``cpml``-cell CPML. Over samples every ``every`` steps,
@@ -771,8 +771,10 @@ def reflection_db(boundary: LearnedBoundary, shape=(64, 64, 64), steps: int = 40
     20 log10(max_t |E_a - E_b| / max_t |E_b|): the wave sent back by the boundary against the
     wave that reached it. epsilon: the small grid's [3] arrays (the large grid extends them by
     edge replication); default vacuum. boundary None: no boundary treatment at all (the grid's
-    edges wrap), on every face. Also returns the same ratio over the whole grid and the
-    series [(step, shell error, shell reference)]."""
+    edges wrap), on every face. cpml_other > 0: the faces without the learned layer carry a
+    CPML of that thickness in both grids (as a deployment that mixes the two would), instead of
+    wrapping. Also returns the same ratio over the whole grid and the series [(step, shell
+    error, shell reference)]."""
     torch = _torch()
     from .simulation import Simulation
     mask = boundary.mask if boundary is not None else FACES_ALL
@@ -789,8 +791,13 @@ def reflection_db(boundary: LearnedBoundary, shape=(64, 64, 64), steps: int = 40
     waves = dipole_pulse(period, pol)
     src = tuple(s // 2 for s in shape) if source is None else tuple(source)
     dt = boundary.net.dt if boundary is not None else DEFAULT_DT
-    small = Simulation(epsilon=[numpy.asarray(e, numpy.float32) for e in epsilon], pmls=[], dt=dt, do_poynting=False)
+    other = [{"axis": "xyz"[a], "polarity": p, "thickness": cpml_other}
+             for a in range(3) for side, p in ((0, "n"), (1, "p"))
+             if cpml_other > 0 and not mask & (1 << (2 * a + side))]
+    small = Simulation(epsilon=[numpy.asarray(e, numpy.float32) for e in epsilon], pmls=[dict(o) for o in other],
+                       dt=dt, do_poynting=False)
     big_pmls = [{"axis": "xyz"[a], "polarity": p, "thickness": cpml} for a in range(3) if pad[a] for p in "np"]
+    big_pmls += [dict(o) for o in other if not pad["xyz".index(o["axis"])]]
     big = Simulation(epsilon=big_eps, pmls=big_pmls, dt=dt, do_poynting=False)
     if boundary is not None:
         boundary.attach(small)
@@ -841,17 +848,19 @@ def reflection_db(boundary: LearnedBoundary, shape=(64, 64, 64), steps: int = 40
 
 
 def evaluate(boundary: LearnedBoundary, shape=(96, 96, 96), steps: int = 400, periods=(20.0, 68.0),
-          stability_shape=(64, 64, 64), stability_steps: int = 3000, threshold_db: float = -40.0,
-          growth_db: float = 0.0):
+             stability_shape=(64, 64, 64), stability_steps: int = 3000, threshold_db: float = -40.0,
+             growth_db: float = 0.0, cpml_other: int = 0):
     """The boundary's verdict: the worst reflection (``reflection_db`` over ``steps`` steps, one
     run per pulse period) and a long run (``stability_steps``) whose shell error, relative to the
     largest field that reached the shell, must stay at most ``growth_db`` at its end (a boundary
     that feeds back its own errors grows them without bound). Accepted when both hold and the
-    reflection is at most ``threshold_db``."""
+    reflection is at most ``threshold_db``. ``cpml_other``: see ``reflection_db``."""
     refl = {}
     for per in periods:
-        refl[per] = reflection_db(boundary, shape=shape, steps=steps, every=10, period=per)["reflection_db"]
-    long = reflection_db(boundary, shape=stability_shape, steps=stability_steps, every=50, period=periods[0])
+        refl[per] = reflection_db(boundary, shape=shape, steps=steps, every=10, period=per,
+                                  cpml_other=cpml_other)["reflection_db"]
+    long = reflection_db(boundary, shape=stability_shape, steps=stability_steps, every=50, period=periods[0],
+                         cpml_other=cpml_other)
     ref = max(r for _, _, r in long["series"]) or 1.0
     t_end, e_end, _ = long["series"][-1]
     end_db = 20 * math.log10(e_end / ref) if e_end > 0 and math.isfinite(e_end) else (math.inf if e_end else -math.inf)

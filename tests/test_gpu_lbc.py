@@ -445,6 +445,16 @@ def test_linear_inference_matches_the_network(mur_training):
         net2.weights("linear")
 
 
+def test_reflection_with_cpml_on_the_other_faces(mur_training):
+    """A learned layer on the z faces with CPML on x and y, as deployed: the thin and the
+    doubled grid both carry the x/y CPML, so the shell error measures the z layer."""
+    L, data, net, mur = mur_training
+    lb = L.LearnedBoundary(mur, "f32", faces=["-z", "+z"])
+    r = L.reflection_db(lb, shape=(24, 24, 24), steps=60, every=4, period=14.0, cpml=8, shell=4, cpml_other=6)
+    assert r["big_shape"] == (24, 24, 48)
+    assert math.isfinite(r["reflection_db"]) and r["reflection_db"] < 0.0
+
+
 def test_evaluation_and_fallback(small_training):
     """The evaluation's verdict decides between the learned layer and CPML."""
     L, data, net, before, start, after = small_training
