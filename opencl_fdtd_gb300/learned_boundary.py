@@ -710,11 +710,15 @@ class LearnedBoundary:
                                             W.data_ptr(),
                                             pred.data_ptr(), pred.numel()))
         self._attached[id(sim)] = (sim, pred, W)
+        # the plan keeps raw pointers to W and pred: the simulation holds them (and this
+        # boundary) until detach, whatever happens to the caller's references
+        sim._lbc_keep = (self, pred, W)
         return sim
 
     def detach(self, sim):
         _lib.check(sim._lib.fdtd_lbc_attach(sim._plan, 0, 0, 0.0, None, None, 0))
         self._attached.pop(id(sim), None)
+        sim._lbc_keep = None
 
     def predict(self, sim, side: int = -1, pred=None, stream=None):
         """Ghost values [ncol][6] of the faces of ``side`` (-1: all) from sim's current state
