@@ -48,6 +48,11 @@ __device__ __forceinline__ uint64_t cell_of(const LGrid &g, const LFace &f, uint
     return ((uint64_t)c[0] * g.s[1] + c[1]) * g.s[2] + c[2];
 }
 
+__device__ __forceinline__ bool in_window(const LGrid &g, int fi, uint32_t u, uint32_t v)
+{
+    return u >= g.win[fi][0] && u < g.win[fi][1] && v >= g.win[fi][2] && v < g.win[fi][3];
+}
+
 __device__ __forceinline__ int face_of(const LGrid &g, uint32_t col)
 {
     int f = 0;
@@ -280,6 +285,11 @@ __global__ void __launch_bounds__(T_APPLY) k_lbc_predict32(const LGrid g, int si
     if (c >= f.ncol) return;
     const uint32_t u = f.u0 + c / f.nv, v = f.v0 + c % f.nv;
     float *out = pred + (uint64_t)(f.col0 + c) * LBC_OUT;
+    if (!in_window(g, fi, u, v)) {
+#pragma unroll
+        for (int o = 0; o < LBC_OUT; ++o) out[o] = memory * out[o];
+        return;
+    }
     // layer 1 is linear in the inputs: accumulate W1^T x on the raw stencil while summing its
     // squares, then scale by 1/r (the normalisation) and add the bias
     float a[LBC_HID], h[LBC_HID];
@@ -346,6 +356,12 @@ __global__ void __launch_bounds__(T_APPLY) k_lbc_predict_lin(const LGrid g, int 
     const uint32_t c = blockIdx.x * T_APPLY + threadIdx.x;
     if (c >= f.ncol) return;
     const uint32_t u = f.u0 + c / f.nv, v = f.v0 + c % f.nv;
+    if (!in_window(g, blockIdx.y, u, v)) {
+        float *out = pred + (uint64_t)(f.col0 + c) * LBC_OUT;
+#pragma unroll
+        for (int o = 0; o < LBC_OUT; ++o) out[o] = memory * out[o];
+        return;
+    }
     float acc[LBC_OUT];
 #pragma unroll
     for (int o = 0; o < LBC_OUT; ++o) acc[o] = 0.f;
@@ -496,9 +512,10 @@ __global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid 
         {
             const int row = lane >> 1, d = lane & 1;
             const uint32_t c = cbase + row;
-            const bool ok = c < f.ncol;
-            const uint32_t cc = ok ? c : cbase;
+            const uint32_t cc = c < f.ncol ? c : cbase;
             const uint32_t u = f.u0 + cc / f.nv, v = f.v0 + cc % f.nv;
+            // columns outside the window read nothing: r = 0, no network term
+            const bool ok = c < f.ncol && in_window(g, blockIdx.y, u, v);
             float x[54];
             float ss = 0.f;
 #pragma unroll
@@ -704,9 +721,26 @@ LGrid lbc_grid(const uint32_t s[3], int face_mask)
             g.nown += o.ncol;
             g.face[g.nface] = f;
             g.own[g.nface] = o;
+            g.win[g.nface][0] = 0;
+            g.win[g.nface][1] = s[ua];
+            g.win[g.nface][2] = 0;
+            g.win[g.nface][3] = s[va];
             ++g.nface;
             owned[a][side] = true;
         }
+    return g;
+}
+
+LGrid lbc_grid_window(const uint32_t s[3], int face_mask, const uint32_t lo[3], const uint32_t hi[3])
+{
+    LGrid g = lbc_grid(s, face_mask);
+    for (int i = 0; i < g.nface; ++i) {
+        const int a = g.face[i].axis, ua = a == 0 ? 1 : 0, va = a == 2 ? 1 : 2;
+        g.win[i][0] = lo[ua] < s[ua] ? lo[ua] : s[ua];
+        g.win[i][1] = hi[ua] < s[ua] ? s[ua] - hi[ua] : 0;
+        g.win[i][2] = lo[va] < s[va] ? lo[va] : s[va];
+        g.win[i][3] = hi[va] < s[va] ? s[va] - hi[va] : 0;
+    }
     return g;
 }
 

@@ -54,9 +54,15 @@ struct LGrid {
     LFace own[6];
     uint32_t ncol;               // columns of all faces
     uint32_t nown;               // outer cells
+    // per face (order of face[]): the columns the network predicts, u in [win[f][0], win[f][1])
+    // and v in [win[f][2], win[f][3]); outside (inside another face's CPML) the ghost is zero
+    uint32_t win[6][4];
 };
 
 LGrid lbc_grid(const uint32_t s[3], int face_mask);
+// the same with the columns that lie inside the CPML of other faces (thickness lo[a] / hi[a] at
+// index 0 / s - 1 of axis a) left to zero ghosts
+LGrid lbc_grid_window(const uint32_t s[3], int face_mask, const uint32_t lo[3], const uint32_t hi[3]);
 cudaError_t launch_lbc_gather(const LGrid &g, const float *E, const float *H, float *X, float *R, float *C,
                               cudaStream_t st);
 cudaError_t launch_mlp_fwd(const float *P, const float *X, int B, float *Y, float *A1, float *A2, float *H1,

@@ -36,10 +36,18 @@ LGrid grid_of(const int32_t shape[3], int32_t mask)
 
 namespace fdtd {
 
+// the plan's learned faces, with the columns inside its CPML faces left to zero ghosts
 static LGrid plan_grid(const FdtdPlan *p)
 {
     const uint32_t s[3] = {p->sx, p->sy, p->sz};
-    return lbc_grid(s, p->lbc_mask);
+    uint32_t lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int f = 0; f < p->d.n_pml; ++f) {
+        const FdtdPmlDesc &pd = p->d.pml[f];
+        if (pd.thickness <= 0) continue;
+        if (pd.polarity == 0) lo[pd.axis] = (uint32_t)pd.thickness;
+        else hi[pd.axis] = (uint32_t)pd.thickness;
+    }
+    return lbc_grid_window(s, p->lbc_mask, lo, hi);
 }
 
 int lbc_before_e(const FdtdPlan *p, const FdtdBuffers *b, const void *H, cudaStream_t st)
