@@ -373,7 +373,10 @@ int fdtd_lbc_fix(const int32_t shape[3], int32_t face_mask, int32_t fields, cons
                  const float *ce, const float *cm, double dt, void *stream);
 /* Make fdtd_run step the plan with the learned boundary (float32 plans with unit cells and no
  * Bloch boundaries; face_mask 0 detaches). weights and pred (ncol x 6 floats) stay owned by
- * the caller and must outlive the attachment. The faces in face_mask should carry no CPML. */
+ * the caller and must outlive the attachment. The faces in face_mask should carry no CPML;
+ * columns of a learned face that lie inside the plan's other CPML faces get zero ghosts in
+ * fdtd_run (fdtd_lbc_predict, which has no plan, predicts every column: a caller stepping by
+ * hand zeroes those rows itself). */
 int fdtd_lbc_attach(FdtdPlan *plan, int32_t face_mask, int32_t precision, float memory, const void *weights,
                     float *pred, int64_t pred_floats);
 

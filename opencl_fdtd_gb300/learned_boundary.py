@@ -736,7 +736,44 @@ class LearnedBoundary:
         _lib.check(sim._lib.fdtd_lbc_predict(_shape_arg(sim.shape), self.mask, int(side), PRECISIONS[self.precision],
                                              self.net.memory, W.data_ptr(), sim.E.data_ptr(), sim.H.data_ptr(),
                                              pred.data_ptr(), pred.numel(), ctypes.c_void_p(st.cuda_stream)))
+        outside = self._outside_rows(sim)
+        if outside is not None:
+            with torch.cuda.stream(st):
+                pred[outside] = 0.0
         return pred
+
+    def _outside_rows(self, sim):
+        """Rows of the columns that lie inside the simulation's CPML faces (fdtd_run gives them
+        zero ghosts; the plan-free predict call does not know the CPML), or None."""
+        torch = _torch()
+        key = ("rows", id(sim))
+        if key in self._pred:
+            return self._pred[key]
+        lo, hi = [0, 0, 0], [0, 0, 0]
+        for pml in sim.pmls:
+            a = "xyz".index(pml["axis"])
+            if pml["polarity"] == "n":
+                lo[a] = int(pml["thickness"])
+            else:
+                hi[a] = int(pml["thickness"])
+        rows = None
+        if any(lo) or any(hi):
+            _, off = columns(sim.shape, self.mask)
+            sel = []
+            for f in range(6):
+                if off[f] < 0:
+                    continue
+                a = f // 2
+                ua, va = [r for r in range(3) if r != a]
+                u = torch.arange(sim.shape[ua]).view(-1, 1).expand(sim.shape[ua], sim.shape[va])
+                v = torch.arange(sim.shape[va]).view(1, -1).expand(sim.shape[ua], sim.shape[va])
+                out = (u < lo[ua]) | (u >= sim.shape[ua] - hi[ua]) | (v < lo[va]) | (v >= sim.shape[va] - hi[va])
+                sel.append(torch.nonzero(out.flatten()).flatten() + off[f])
+            rows = torch.cat(sel).to(sim.device) if sel else None
+            if rows is not None and rows.numel() == 0:
+                rows = None
+        self._pred[key] = rows
+        return rows
 
     def fix(self, sim, pred, fields: str, stream=None):
         """The fix-up of the outermost cells' updates: 'E' right after update_E, 'H' after

@@ -3,6 +3,7 @@ and Adam kernels against the float64 CPU oracle (oracle/lbc.py); the tensor-core
 against the float32 one; the boundary step of fdtd_run against the same step made by hand; a
 short training run that lowers the loss and absorbs better than the thin layer without the
 network; and the CPML fallback."""
+import copy
 import ctypes
 import math
 
@@ -282,6 +283,26 @@ def test_run_with_boundary_equals_manual_steps(precision, memory):
     c = Simulation(**_sim_kwargs(shape, 12))
     c.run(6, point_sources=[(src, vals)])
     assert not torch.equal(a.E, c.E)
+
+
+def test_run_with_cpml_on_other_faces_equals_manual_steps():
+    """A learned layer on the z faces with CPML on x and y: fdtd_run (zero ghosts for the
+    columns inside the CPML) and the hand-made steps agree bit for bit."""
+    from opencl_fdtd_gb300 import Simulation
+    L = _L()
+    shape = (16, 14, 12)
+    net = _net(17, 50.0)
+    lb = L.LearnedBoundary(net, "f32", faces=["-z", "+z"])
+    kw = _sim_kwargs(shape, 18)
+    kw["pmls"] = [{"axis": a, "polarity": p, "thickness": 3} for a in "xy" for p in "np"]
+    a = Simulation(**copy.deepcopy(kw))
+    b = Simulation(**copy.deepcopy(kw))
+    lb.attach(a)
+    a.run(5)
+    for _ in range(5):
+        lb.step(b)
+    torch.cuda.synchronize()
+    assert torch.equal(a.E, b.E) and torch.equal(a.H, b.H)
 
 
 def test_boundary_on_the_hs_path_matches_plain_path():
