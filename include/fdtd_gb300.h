@@ -218,6 +218,11 @@ int fdtd_plane_sum_noalloc(FdtdPlan *plan, const void *field, int32_t component,
 int fdtd_energy(FdtdPlan *plan, const FdtdBuffers *buf, double *scratch, int32_t scratch_len,
                 double *out, void *stream);
 
+/* Field watchdog: *count (a device uint32, cleared here) receives the number of NaN / Inf
+ * values in E and H (and F, G with Bloch boundaries), on the stream; a caller that finds it
+ * nonzero reports FDTD_ERR_NONFINITE. No trap, no host wait inside. */
+int fdtd_count_nonfinite(FdtdPlan *plan, const FdtdBuffers *buf, uint32_t *count, void *stream);
+
 /* Run nsteps canonical steps (fdtd.py:162-175: E, F, point sources, H, G, S) on the stream
  * with no host round trip. src and mon may be NULL; mon is sampled after every step and its
  * step / series_row advance by nsteps. With the scratch buffers set (and no Bloch

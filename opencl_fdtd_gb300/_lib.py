@@ -109,6 +109,7 @@ SIGNATURES = [
     ("fdtd_monitor_sample", c_i32, [c_vp, _P(FdtdBuffers), c_vp, _P(FdtdDftMonitor)]),
     ("fdtd_plane_sum", c_i32, [c_vp, c_vp, c_i32, c_i32, c_i64, c_vp, c_i32, c_vp, c_vp]),
     ("fdtd_energy", c_i32, [c_vp, _P(FdtdBuffers), c_vp, c_i32, c_vp, c_vp]),
+    ("fdtd_count_nonfinite", c_i32, [c_vp, _P(FdtdBuffers), c_vp, c_vp]),
     ("fdtd_plane_sum_noalloc", c_i32, [c_vp, c_vp, c_i32, c_i32, c_i64, c_i32, c_vp, c_vp]),
     ("fdtd_run", c_i32, [c_vp, _P(FdtdBuffers), c_vp, c_i32, _P(FdtdPointSources),
                          _P(FdtdDftMonitor)]),

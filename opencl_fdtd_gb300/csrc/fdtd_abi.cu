@@ -1027,6 +1027,33 @@ int fdtd_energy(FdtdPlan *p, const FdtdBuffers *b, double *scratch, int32_t scra
                                   : energy_t<float>(p, b, scratch, nblk, out, st);
 }
 
+}  // extern "C"
+
+template <typename R>
+static int count_nonfinite_t(FdtdPlan *p, const FdtdBuffers *b, uint32_t *count, cudaStream_t st)
+{
+    int rc = check_cuda(cudaMemsetAsync(count, 0, sizeof(uint32_t), st), "watchdog clear");
+    const void *fields[4] = {b->E, b->H, p->d.n_bloch ? b->F : nullptr, p->d.n_bloch ? b->G : nullptr};
+    for (int f = 0; !rc && f < 4; ++f)
+        if (fields[f])
+            rc = check_cuda(launch_count_nonfinite<R>((const R *)fields[f], 3 * p->N, (unsigned int *)count, st),
+                            "watchdog launch");
+    return rc;
+}
+
+extern "C" {
+
+int fdtd_count_nonfinite(FdtdPlan *p, const FdtdBuffers *b, uint32_t *count, void *stream)
+{
+    int rc = check_common(p, b);
+    if (rc) return rc;
+    if (!b->E || !b->H) return fail(FDTD_ERR_INVALID, "count_nonfinite: E and H are required");
+    if (p->d.n_bloch && (!b->F || !b->G)) return fail(FDTD_ERR_INVALID, "count_nonfinite: F and G are required");
+    if (!count) return fail(FDTD_ERR_INVALID, "count_nonfinite: count is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == FDTD_F64 ? count_nonfinite_t<double>(p, b, count, st) : count_nonfinite_t<float>(p, b, count, st);
+}
+
 int fdtd_run(FdtdPlan *p, const FdtdBuffers *b, void *stream, int32_t nsteps,
              const FdtdPointSources *src, FdtdDftMonitor *mon)
 {

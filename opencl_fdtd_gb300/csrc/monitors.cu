@@ -123,6 +123,31 @@ cudaError_t launch_energy(const EnergyK<R> &k, int nblocks, double *out, cudaStr
     return cudaGetLastError();
 }
 
+// field watchdog: every thread counts the non-finite values of its grid-stride slice, the warp
+// sums its lanes' counts, one atomic per warp that found any
+template <typename R>
+__global__ void __launch_bounds__(RED_THREADS) k_count_nonfinite(const R *a, uint64_t n, unsigned int *count)
+{
+    unsigned int local = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        local += isfinite(a[i]) ? 0u : 1u;
+    local = __reduce_add_sync(0xffffffffu, local);
+    if ((threadIdx.x & 31u) == 0 && local) atomicAdd(count, local);
+}
+
+template <typename R>
+cudaError_t launch_count_nonfinite(const R *a, uint64_t n, unsigned int *count, cudaStream_t st)
+{
+    if (!n) return cudaSuccess;
+    const uint64_t want = (n + RED_THREADS - 1) / RED_THREADS;
+    const int blocks = (int)(want < 2048 ? want : 2048);
+    k_count_nonfinite<R><<<blocks, RED_THREADS, 0, st>>>(a, n, count);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_count_nonfinite<float>(const float *, uint64_t, unsigned int *, cudaStream_t);
+template cudaError_t launch_count_nonfinite<double>(const double *, uint64_t, unsigned int *, cudaStream_t);
 template cudaError_t launch_dft<float>(const DftK<float> &, cudaStream_t);
 template cudaError_t launch_dft<double>(const DftK<double> &, cudaStream_t);
 template cudaError_t launch_plane_sum<float>(const PlaneRedK<float> &, int, double *, cudaStream_t);

@@ -40,5 +40,8 @@ template <typename R>
 cudaError_t launch_plane_sum(const PlaneRedK<R> &k, int nblocks, double *out, cudaStream_t st);
 template <typename R>
 cudaError_t launch_energy(const EnergyK<R> &k, int nblocks, double *out, cudaStream_t st);
+// adds the number of NaN / Inf values among a[0 .. n) to *count (device)
+template <typename R>
+cudaError_t launch_count_nonfinite(const R *a, uint64_t n, unsigned int *count, cudaStream_t st);
 
 }  // namespace fdtd

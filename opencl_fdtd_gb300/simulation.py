@@ -464,8 +464,12 @@ class Simulation:
     # additions beyond the reference
     # ------------------------------------------------------------------------------------
     def run(self, nsteps: int, point_sources=None, wait_for=None, monitor=None,
-            path: str = "auto") -> Event:
+            path: str = "auto", watchdog: int = 0) -> Event:
         """Advance ``nsteps`` canonical steps (E, F, point sources, H, G, S) in one call.
+
+        ``watchdog`` > 0 runs the steps in chunks of that many and counts the non-finite
+        field values on the device after each chunk (``nonfinite_count``); the first chunk
+        that leaves any raises FloatingPointError with the step reached.
 
         ``point_sources`` is a list of (flat_index, values) pairs: after the E update of step
         t, ``E[flat_index] += values[t]`` (fdtd.py:168-169 without the host round trip).
@@ -480,6 +484,8 @@ class Simulation:
           'fused'  E, sources, H and S in one kernel per step (no Bloch boundaries).
         The 'hs' and 'fused' paths write oS on the last step only."""
         nsteps = int(nsteps)
+        if watchdog and int(watchdog) > 0:
+            return self._run_watched(nsteps, int(watchdog), point_sources, wait_for, monitor, path)
         stream = self._stream_handle(wait_for)
         src = None
         keep = []
@@ -526,6 +532,32 @@ class Simulation:
             t.record_stream(stream)
         self.steps_run += nsteps
         return Event(stream)
+
+    def _run_watched(self, nsteps, every, point_sources, wait_for, monitor, path):
+        ev = None
+        for t0 in range(0, nsteps, every):
+            n = min(every, nsteps - t0)
+            sub = None
+            if point_sources:
+                sub = [(i, numpy.asarray(v, dtype=numpy.float64).ravel()[t0:t0 + n]) for i, v in point_sources]
+            ev = self.run(n, point_sources=sub, wait_for=wait_for if t0 == 0 else None, monitor=monitor, path=path)
+            bad = self.nonfinite_count()
+            if bad:
+                raise FloatingPointError("%d non-finite field values after step %d" % (bad, self.steps_run))
+        return ev
+
+    def nonfinite_count(self) -> int:
+        """Number of NaN / Inf values in E and H (and F, G), counted on the device
+        (fdtd_count_nonfinite) and read back (waits for the simulation's stream)."""
+        if getattr(self, "_nf", None) is None:
+            self._nf = torch.zeros(1, dtype=torch.int32, device=self.device)
+        _lib.check(self._lib.fdtd_count_nonfinite(self._plan, ctypes.byref(self._buffers()), self._nf.data_ptr(),
+                                                  ctypes.c_void_p(self.queue.cuda_stream)))
+        self.queue.synchronize()
+        return int(self._nf.item())
+
+    def check_finite(self) -> bool:
+        return self.nonfinite_count() == 0
 
     # ---- FP64 monitors --------------------------------------------------------------------
     def dft_monitor(self, points, omegas=(), record: bool = True, t0: int = None):
