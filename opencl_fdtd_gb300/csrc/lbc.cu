@@ -130,7 +130,6 @@ __global__ void __launch_bounds__(T_FWD) k_mlp_fwd(const float *P, const float *
     }
 #pragma unroll
     for (int j = 0; j < LBC_HID; ++j) a[j] = w[LBC_B2 + j];
-#pragma unroll
     for (int k = 0; k < LBC_HID; ++k) {
         const float hk = h[k];
 #pragma unroll
@@ -296,11 +295,13 @@ __global__ void __launch_bounds__(T_APPLY) k_lbc_predict32(const LGrid g, int si
 #pragma unroll
     for (int j = 0; j < LBC_HID; ++j) a[j] = 0.f;
     float ss = 0.f;
-#pragma unroll
+    // the 18 stencil cells as a runtime loop (unrolling them with the 64-wide inner products
+    // multiplies the code and the compile time for a kernel that only checks the others)
+#pragma unroll 1
     for (int d = 0; d < 2; ++d)
-#pragma unroll
+#pragma unroll 1
         for (int du = -1; du <= 1; ++du)
-#pragma unroll
+#pragma unroll 1
             for (int dv = -1; dv <= 1; ++dv) {
                 const uint64_t i = cell_of(g, f, u, v, d, du, dv);
                 const int k0 = ((d * 3 + (du + 1)) * 3 + (dv + 1)) * 6;
@@ -325,7 +326,6 @@ __global__ void __launch_bounds__(T_APPLY) k_lbc_predict32(const LGrid g, int si
     for (int j = 0; j < LBC_HID; ++j) h[j] = gelu(a[j]);
 #pragma unroll
     for (int j = 0; j < LBC_HID; ++j) a[j] = w[LBC_B2 + j];
-#pragma unroll
     for (int k = 0; k < LBC_HID; ++k) {
         const float hk = h[k];
 #pragma unroll
