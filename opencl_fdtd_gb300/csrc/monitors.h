@@ -28,6 +28,22 @@ struct PlaneRedK {
     uint64_t ncell, inner, base, stride_a, stride_b;
 };
 
+// Arguments of the plane sum of component ``comp`` of a 3N field over the plane ``plane``
+// normal to ``axis`` on an (sx, sy, sz) grid; the one mapping both plane-sum entry points use.
+template <typename R>
+inline PlaneRedK<R> plane_red_args(const void *field, int comp, int axis, int64_t plane,
+                                   uint64_t sx, uint64_t sy, uint64_t sz, double *partial)
+{
+    PlaneRedK<R> k;
+    const uint64_t syz = sy * sz;
+    k.src = (const R *)field + (uint64_t)comp * sx * syz;
+    k.partial = partial;
+    if (axis == 0) { k.base = plane * syz; k.stride_a = sz; k.stride_b = 1; k.inner = sz; k.ncell = syz; }
+    else if (axis == 1) { k.base = plane * sz; k.stride_a = syz; k.stride_b = 1; k.inner = sz; k.ncell = sx * sz; }
+    else { k.base = plane; k.stride_a = syz; k.stride_b = sz; k.inner = sy; k.ncell = sx * sy; }
+    return k;
+}
+
 template <typename R>
 struct EnergyK {
     const R *E, *H, *eps, *mu;

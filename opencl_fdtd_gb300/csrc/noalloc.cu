@@ -58,13 +58,8 @@ template <typename R>
 int plane_sum_static(const FdtdPlan *p, const void *field, int comp, int axis, int64_t plane,
                      double *partials, int nblocks, double *out, cudaStream_t st)
 {
-    fdtd::PlaneRedK<R> k;
-    k.src = (const R *)field + (uint64_t)comp * p->N;
-    k.partial = partials;
-    const uint64_t sx = p->sx, sy = p->sy, sz = p->sz, syz = p->syz;
-    if (axis == 0) { k.base = plane * syz; k.stride_a = sz; k.stride_b = 1; k.inner = sz; k.ncell = syz; }
-    else if (axis == 1) { k.base = plane * sz; k.stride_a = syz; k.stride_b = 1; k.inner = sz; k.ncell = sx * sz; }
-    else { k.base = plane; k.stride_a = syz; k.stride_b = sz; k.inner = sy; k.ncell = sx * sy; }
+    const fdtd::PlaneRedK<R> k =
+        fdtd::plane_red_args<R>(field, comp, axis, plane, p->sx, p->sy, p->sz, partials);
     return fdtd::check_cuda(fdtd::launch_plane_sum<R>(k, nblocks, out, st), "plane sum (no-alloc) launch");
 }
 

@@ -40,11 +40,15 @@ class DftMonitor:
         if om.size == 0 and not record:
             raise ValueError("a monitor needs frequencies or a recorded series")
         dev = sim.device
-        self.index = torch.from_numpy(idx).to(dev)
-        self.omega = torch.from_numpy(om).to(dev) if om.size else torch.zeros(1, dtype=torch.float64, device=dev)
-        self.accum = torch.zeros((idx.size, max(om.size, 1), 2), dtype=torch.float64, device=dev)
+        # Every buffer the kernels touch is made (and zeroed) on the simulation's queue, the
+        # stream its kernels run on, so the first run is ordered after the zeroing whatever
+        # torch's current stream is.
+        with torch.cuda.stream(sim.queue):
+            self.index = torch.from_numpy(idx).to(dev)
+            self.omega = torch.from_numpy(om).to(dev) if om.size else torch.zeros(1, dtype=torch.float64, device=dev)
+            self.accum = torch.zeros((idx.size, max(om.size, 1), 2), dtype=torch.float64, device=dev)
+            self._series = torch.zeros((0, idx.size), dtype=torch.float64, device=dev)
         self.record = record
-        self._series = torch.zeros((0, idx.size), dtype=torch.float64, device=dev)
         self.n_freq = int(om.size)
         self.samples = 0
         self.t0 = int(t0)
@@ -55,10 +59,14 @@ class DftMonitor:
             return
         need = self.samples + more
         if need > self._series.shape[0]:
+            # Grow on the queue: the copy then follows the queued kernels that write the old
+            # rows, and the caching allocator does not hand the old buffer to another stream
+            # while those kernels may still write it.
             cap = max(need, 2 * self._series.shape[0], 1024)
-            grown = torch.zeros((cap, self._series.shape[1]), dtype=torch.float64, device=self.sim.device)
-            if self.samples:
-                grown[:self.samples] = self._series[:self.samples]
+            with torch.cuda.stream(self.sim.queue):
+                grown = torch.zeros((cap, self._series.shape[1]), dtype=torch.float64, device=self.sim.device)
+                if self.samples:
+                    grown[:self.samples] = self._series[:self.samples]
             self._series = grown
 
     def struct(self, more: int) -> _lib.FdtdDftMonitor:

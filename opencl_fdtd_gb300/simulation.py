@@ -534,6 +534,14 @@ class Simulation:
         return Event(stream)
 
     def _run_watched(self, nsteps, every, point_sources, wait_for, monitor, path):
+        if nsteps <= 0:
+            return self.run(nsteps, point_sources=point_sources, wait_for=wait_for,
+                            monitor=monitor, path=path)
+        for k, (_, v) in enumerate(point_sources or ()):
+            size = numpy.asarray(v, dtype=numpy.float64).size
+            if size < nsteps:
+                # the whole run is checked before the first chunk moves the fields
+                raise ValueError("point source {} has {} values for {} steps".format(k, size, nsteps))
         ev = None
         for t0 in range(0, nsteps, every):
             n = min(every, nsteps - t0)

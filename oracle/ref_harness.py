@@ -21,9 +21,11 @@ runs it unmodified, with only the OpenCL runtime replaced:
   scalar returns a Python float; ``dt`` and ``kappa_max`` then stay weak scalars and every
   table is computed in float32 arithmetic, as under numpy 1.x.
 
-It needs the reference source tree (``OPENCL_FDTD_REF``, default the mounted checkout) and
-jinja2; it is used in this container to pin the C restatement (fdtd_port.c) and to write the
-golden fixtures under tests/golden/. ``export_replay`` also saves a rendered case (C sources,
+It needs the reference source tree and jinja2. The tree is ``$OPENCL_FDTD_REF`` when that is
+set, else a checkout named ``reference`` beside this repository's folder (``../reference``
+relative to the repository root); without either, ``available()`` is False and the tests that
+need the reference skip. It pins the C restatement (fdtd_port.c) and writes the golden
+fixtures under tests/golden/. ``export_replay`` also saves a rendered case (C sources,
 argument manifest, coefficient tables) so that ``ref_replay`` can run the reference kernels
 where the source tree is absent.
 """
@@ -40,8 +42,9 @@ import types
 
 import numpy
 
-REF_ROOT = os.environ.get("OPENCL_FDTD_REF", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT = os.environ.get("OPENCL_FDTD_REF") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference")
 REF_OUT = os.path.join(HERE, "_ref")
 
 _CTYPE = {

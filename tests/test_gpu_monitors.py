@@ -101,3 +101,33 @@ def test_standing_wave_frequency_matches_yee_dispersion():
     e0 = mean_energy()
     g.run(1000)
     assert abs(mean_energy() - e0) / e0 < 2e-3
+
+
+def test_monitor_on_own_queue_grows_in_order():
+    """A monitor on a simulation with its own stream, recorded past its first 1024-row
+    buffer while steps are still queued: every row equals the same run on torch's default
+    stream, and the series equals per-step samples of the state."""
+    kw, _ = cases.build("periodic_pec_poynting")
+    shape = kw["epsilon"][0].shape
+    N = int(numpy.prod(shape))
+    src = [(int(numpy.ravel_multi_index((3, 4, 5), shape)) + 2 * N,
+            [math.sin(0.2 * t) * math.exp(-0.5 * ((t - 40) / 12) ** 2) for t in range(1400)])]
+    pts = [(2, (3, 4, 5)), (0, (1, 2, 3))]
+    q = torch.cuda.Stream()
+    a = _gpu(queue=q, **copy.deepcopy(kw))
+    mon_a = a.dft_monitor(pts, [0.4])
+    b = _gpu(**copy.deepcopy(kw))
+    mon_b = b.dft_monitor(pts, [0.4])
+    # keep torch's current stream busy so that unordered work on it would show
+    big = torch.empty(64 << 20, device="cuda")
+    for t0, n in ((0, 700), (700, 700)):
+        with torch.cuda.stream(torch.cuda.current_stream()):
+            big.mul_(1.0)
+        sub = [(i, v[t0:t0 + n]) for i, v in src]
+        a.run(n, point_sources=sub, monitor=mon_a)
+        b.run(n, point_sources=sub, monitor=mon_b)
+    sa, sb = mon_a.series(), mon_b.series()
+    assert sa.shape == (1400, 2)
+    assert numpy.array_equal(sa, sb)
+    assert numpy.array_equal(mon_a.spectrum(), mon_b.spectrum())
+    assert numpy.abs(sa).max() > 0
