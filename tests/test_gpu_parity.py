@@ -67,6 +67,13 @@ def test_config1_full_size():
         for comp in range(3):
             assert abs(s["l2"][comp] - gold[k]["l2"][comp]) <= REL_L2_TOL * max(gold[k]["l2"]) + 1e-12
         assert rel_l2(numpy.asarray(s["sample"]), numpy.asarray(gold[k]["sample"])) <= REL_L2_TOL
+    # error of the float32 result against the same 500 steps in float64
+    d = c1_full(_gpu, float_type=numpy.float64)
+    err = {k: float(numpy.linalg.norm(a.astype(numpy.float64) - cases.to_numpy(getattr(d, k))) /
+                    numpy.linalg.norm(cases.to_numpy(getattr(d, k))))
+           for k, a in (("E", ge), ("H", gh))}
+    print("config1 float32 vs float64 relative L2 after 500 steps:", err)
+    assert all(v < 1e-4 for v in err.values()), err
 
 
 @pytest.mark.parametrize("name", ["pml_mixed", "periodic_pec_poynting", "bloch_trivial"])
