@@ -55,8 +55,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--xchunk", type=int, default=0, help="x planes per thread (0: plan default)")
-    ap.add_argument("--fused-cells", type=int, default=0)
+    ap.add_argument("--fused-rows", type=int, default=0)
     ap.add_argument("--fused-xchunk", type=int, default=0)
+    ap.add_argument("--fused-stages", type=int, default=0)
+    ap.add_argument("--fused-tma", type=int, default=-1)
     ap.add_argument("--slab", type=int, default=-1, help="x planes per L2 slab (-1: plan default)")
     ap.add_argument("--hs-xchunk", type=int, default=0)
     ap.add_argument("--hs-prefetch", type=int, default=-1)
@@ -351,10 +353,14 @@ def main():
     sim = Simulation(**kw)
     if args.xchunk:
         sim.tune(xchunk=args.xchunk)
-    if args.fused_cells:
-        sim.tune(fused_cells=args.fused_cells)
+    if args.fused_rows:
+        sim.tune(fused_rows=args.fused_rows)
     if args.fused_xchunk:
         sim.tune(fused_xchunk=args.fused_xchunk)
+    if args.fused_stages:
+        sim.tune(fused_stages=args.fused_stages)
+    if args.fused_tma >= 0:
+        sim.tune(fused_tma=bool(args.fused_tma))
     if args.slab >= 0:
         sim.tune(slab=args.slab)
     if args.hs_xchunk:
@@ -419,7 +425,7 @@ def main():
         nslab = (wl["shape"][0] + sim.slab_planes() - 1) // sim.slab_planes()
         launches = {"fused": K, "hs": 3 * K,
                     "slab": K * ((3 if poynting else 2) * nslab + (3 if poynting else 1) + 1)}[name]
-        kname = {"fused": "k_fused_step", "hs": "step (k_bulk_e + k_bulk_hs)",
+        kname = {"fused": "k_step", "hs": "step (k_bulk_e + k_bulk_hs)",
                  "slab": "step (k_bulk_e/h/s over L2 slabs)"}[name]
         out_paths[name] = {
             "ms_per_step": ms, "value": world * N * K / (total * 1e-3) / 1e6, "gpu_launches": launches,

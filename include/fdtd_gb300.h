@@ -95,11 +95,12 @@ typedef struct FdtdBuffers {
      * filled by fdtd_prepare. When set they must be current; when NULL every cell divides,
      * which is slower but gives the same result. */
     void *ce, *cm;
-    /* Optional scratch of the fused multi-step path of fdtd_run: second copies of E, H and
-     * of every psi_e / psi_h array (same sizes). When all are set, fdtd_run advances each
-     * step with one fused kernel that reads one copy and writes the other; at the end the
-     * result is always back in E, H, psi_e, psi_h. When NULL, fdtd_run uses the per-update
-     * kernels. Results are identical either way. */
+    /* Optional second copies for fdtd_run (same sizes as E, H, psi_e, psi_h). With H2 and every
+     * psi_h2 set (E2 NULL), steps run update_E in place and H and S in one launch that reads
+     * one copy of H and writes the other. With E2, H2 and every psi_e2 / psi_h2 set, each step
+     * is one launch of the one-pass kernel, which reads one copy of everything and writes the
+     * other. At the end the result is always back in E, H, psi_e, psi_h. When NULL, fdtd_run
+     * uses the per-update kernels. Results are identical either way. */
     void *E2, *H2;
     void *psi_e2[6][2], *psi_h2[6][2];
 } FdtdBuffers;
@@ -121,21 +122,42 @@ int fdtd_plan_destroy(FdtdPlan *plan);
  *   XCHUNK        consecutive x planes one thread of the update kernels advances (default 8)
  *   SLAB          x planes per L2-resident slab of fdtd_run's per-update schedule
  *                 (default 0 = whole grid)
- *   FUSED_CELLS   plane cells one block of the fused step owns (0 = the maximum, 768 - 2*sz)
- *   FUSED_XCHUNK  x planes one block of the fused step marches (default 16)
+ *   FUSED_ROWS    own y rows of a tile of the one-pass step (default 0: the most that fit a
+ *                 block, 11 for sz = 73 in float32)
+ *   FUSED_XCHUNK  x planes one block of the one-pass step marches (default 0: whole waves of
+ *                 one block per SM)
+ *   FUSED_STAGES  planes in the one-pass step's shared-memory ring, 2..6 (default 0: 4); fewer
+ *                 when the shared memory of a block cannot hold that many
+ *   FUSED_TMA     1 (default): the one-pass step stages the rows of tiles that do not wrap around
+ *                 the y boundary with bulk asynchronous copies when every staged buffer is
+ *                 16-byte aligned; 0: per-element asynchronous copies everywhere
  *   HS_XCHUNK     x planes one block of the H+S kernel of fdtd_run marches (default 16)
  *   HS_PREFETCH   1: the H+S kernel loads the next plane ahead (one block per SM); 0: not
  *                 (two blocks per SM, the default)
- *   TIMING        1: fdtd_run's H+S path records CUDA events around its update_E and H+S
- *                 kernels on up to 64 steps spread over the call and waits for the stream
- *                 before it returns (profiling; read with fdtd_run_kernel_ms); 0 (default) */
+ *   TIMING        1: fdtd_run records CUDA events around its kernels on up to 64 steps spread
+ *                 over the call (update_E and H+S on the H+S path, the step kernel on the
+ *                 one-pass path) and waits for the stream before it returns (profiling; read
+ *                 with fdtd_run_kernel_ms); 0 (default) */
 #define FDTD_TUNE_XCHUNK 1
 #define FDTD_TUNE_SLAB 2
-#define FDTD_TUNE_FUSED_CELLS 3
+#define FDTD_TUNE_FUSED_ROWS 3
 #define FDTD_TUNE_FUSED_XCHUNK 4
 #define FDTD_TUNE_HS_XCHUNK 5
 #define FDTD_TUNE_HS_PREFETCH 6
 #define FDTD_TUNE_TIMING 7
+#define FDTD_TUNE_FUSED_STAGES 8
+#define FDTD_TUNE_FUSED_TMA 9
+/* Read-only keys of fdtd_plan_get: the path of the last fdtd_run (FDTD_PATH_*) and the tiling
+ * of its last one-pass launch (own rows per tile, x chunk, stages, threads per block). */
+#define FDTD_GET_LAST_RUN_PATH 100
+#define FDTD_GET_STEP_ROWS 101
+#define FDTD_GET_STEP_XCHUNK 102
+#define FDTD_GET_STEP_STAGES 103
+#define FDTD_GET_STEP_THREADS 104
+#define FDTD_PATH_NONE 0
+#define FDTD_PATH_PER_UPDATE 1     /* update_E, sources, update_H, update_S launches */
+#define FDTD_PATH_HS 2             /* update_E in place, sources, H and S in one launch */
+#define FDTD_PATH_ONEPASS 3        /* E, sources, H and S of a step in one launch */
 int fdtd_plan_tune(FdtdPlan *plan, int32_t key, int32_t value);
 /* Current value of a tuning key. */
 int fdtd_plan_get(const FdtdPlan *plan, int32_t key, int32_t *value);
@@ -231,10 +253,17 @@ int fdtd_count_nonfinite(FdtdPlan *plan, const FdtdBuffers *buf, uint32_t *count
 int fdtd_run(FdtdPlan *plan, const FdtdBuffers *buf, void *stream, int32_t nsteps,
              const FdtdPointSources *src, FdtdDftMonitor *mon);
 
-/* Mean launch time in ms of update_E (ms[0]) and of the H+S kernel (ms[1]) over the sampled
- * steps of the last fdtd_run made on the H+S path with FDTD_TUNE_TIMING on, and the number of
- * samples (0 if none). Profiling aid; no counterpart in the reference. */
+/* Mean launch time in ms over the sampled steps of the last fdtd_run made with FDTD_TUNE_TIMING
+ * on: update_E (ms[0]) and the H+S kernel (ms[1]) on the H+S path, the step kernel (ms[0]; ms[1]
+ * = 0) on the one-pass path; and the number of samples (0 if none). Profiling aid; no
+ * counterpart in the reference. */
 int fdtd_run_kernel_ms(const FdtdPlan *plan, double ms[2], int32_t *samples);
+
+/* Device status of the plan's kernels: every wait for staged data inside the one-pass step is
+ * bounded, and one that runs out sets a bit here (4) and ends its block. Waits for the stream,
+ * stores the bits in *bits, clears them and returns FDTD_ERR_WATCHDOG when any was set. No
+ * counterpart in the reference. */
+int fdtd_device_status(FdtdPlan *plan, void *stream, int32_t *bits);
 
 /* ---- batched stepping of many independent variants (one persistent launch) ---------------
  * No counterpart in the reference, which steps one grid per Simulation. Each variant is a

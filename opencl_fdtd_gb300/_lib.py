@@ -25,11 +25,22 @@ FDTD_F32 = 0
 FDTD_F64 = 1
 FDTD_TUNE_XCHUNK = 1
 FDTD_TUNE_SLAB = 2
-FDTD_TUNE_FUSED_CELLS = 3
+FDTD_TUNE_FUSED_ROWS = 3
 FDTD_TUNE_FUSED_XCHUNK = 4
 FDTD_TUNE_HS_XCHUNK = 5
 FDTD_TUNE_HS_PREFETCH = 6
 FDTD_TUNE_TIMING = 7
+FDTD_TUNE_FUSED_STAGES = 8
+FDTD_TUNE_FUSED_TMA = 9
+FDTD_GET_LAST_RUN_PATH = 100
+FDTD_GET_STEP_ROWS = 101
+FDTD_GET_STEP_XCHUNK = 102
+FDTD_GET_STEP_STAGES = 103
+FDTD_GET_STEP_THREADS = 104
+FDTD_PATH_NONE = 0
+FDTD_PATH_PER_UPDATE = 1
+FDTD_PATH_HS = 2
+FDTD_PATH_ONEPASS = 3
 
 
 class FdtdPmlDesc(ctypes.Structure):
@@ -114,6 +125,7 @@ SIGNATURES = [
     ("fdtd_run", c_i32, [c_vp, _P(FdtdBuffers), c_vp, c_i32, _P(FdtdPointSources),
                          _P(FdtdDftMonitor)]),
     ("fdtd_run_kernel_ms", c_i32, [c_vp, _P(c_f64), _P(c_i32)]),
+    ("fdtd_device_status", c_i32, [c_vp, c_vp, _P(c_i32)]),
     ("fdtd_batch_create", c_i32, [_P(FdtdBatchVariant), c_i32, c_i32, c_i64, _P(c_vp)]),
     ("fdtd_batch_destroy", c_i32, [c_vp]),
     ("fdtd_batch_tune", c_i32, [c_vp, c_i32, c_i32]),

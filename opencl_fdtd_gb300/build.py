@@ -30,7 +30,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 # contraction so that they keep the reference's rounding.
 UNITS = {
     "yee_kernels.cu": ["--fmad=false"],
-    "step_fused.cu": ["--fmad=false"],
+    "step_kernel.cu": ["--fmad=false"],
     "hs_fused.cu": ["--fmad=false"],
     "batch.cu": ["--fmad=false"],
     "batch_abi.cu": [],

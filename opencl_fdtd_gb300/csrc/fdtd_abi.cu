@@ -14,7 +14,7 @@
 #include "yee_common.cuh"
 #include "yee_launch.h"
 #include "fdtd_plan.h"
-#include "fused.h"
+#include "step.h"
 #include "monitors.h"
 #include "hs_fused.h"
 
@@ -481,65 +481,20 @@ int run_slabs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
     return FDTD_OK;
 }
 
-// Cells of a plane one fused-step block owns: its window (own cells plus one row of sz cells
-// on each side) must fit the block's FUSED_THREADS threads. 0 when a plane row is too long.
-uint32_t fused_cells_of(const FdtdPlan *p)
-{
-    if ((uint64_t)2 * p->sz + 32 > (uint64_t)FUSED_THREADS) return 0;
-    uint32_t J = FUSED_THREADS - 2 * p->sz;
-    if (p->fused_cells && p->fused_cells < J) J = p->fused_cells;
-    return J < p->syz ? J : p->syz;
-}
+// ---- one-pass step (step_kernel.cu) -------------------------------------------------------
+bool aligned16(const void *q) { return ((uintptr_t)q & 15u) == 0; }
 
-// Fused multi-step path: one launch per step, reading A and writing B, then swapping.
+// CPML faces of the one-pass step (a 'p' face thicker than its axis never applies) and the plan's
+// face index per axis and side (-1: none).
 template <typename R>
-int run_fused(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
-              const FdtdPointSources *src, const FdtdDftMonitor *mon)
+void step_faces(const FdtdPlan *p, StepK<R> &k, int fidx[3][2])
 {
-    FusedK<R> k;
-    std::memset(&k, 0, sizeof(k));
-    k.sx = p->sx;
-    k.sy = p->sy;
-    k.sz = p->sz;
-    k.syz = p->syz;
-    k.N = p->N;
-    k.dsz = FastDiv::make(p->sz);
-    k.dt = (R)p->d.dt;
-    k.inv_d = (R)(1.0 / p->d.dx);
-    k.sf = (R)((double)k.dt * 0.125);
-    for (int r = 0; r < 3; ++r) {
-        k.inv_de[r] = p->d.uniform ? nullptr : (const R *)b->inv_de[r];
-        k.inv_dh[r] = p->d.uniform ? nullptr : (const R *)b->inv_dh[r];
-    }
-    const int dxmode = !p->d.uniform ? 2 : ((R)(1.0 / p->d.dx) == R(1) ? 0 : 1);
-    k.ce = (const R *)b->ce;
-    k.cm = p->d.has_mu ? (const R *)b->cm : nullptr;
-    k.S = (R *)b->S;
-    k.oS = (R *)b->oS;
-    const bool poynt = p->d.do_poynting != 0;
-    if (src && src->n > 0) {
-        k.nsrc = src->n;
-        k.src_values = (const R *)src->values;
-        for (int s = 0; s < src->n; ++s) {
-            const uint64_t ind = (uint64_t)src->index[s];
-            const uint64_t cell = ind % p->N;
-            k.src_c[s] = (int32_t)(ind / p->N);
-            k.src_x[s] = (uint32_t)(cell / p->syz);
-            k.src_y[s] = (uint32_t)((cell % p->syz) / p->sz);
-            k.src_z[s] = (uint32_t)(cell % p->sz);
-        }
-    }
-    k.J = fused_cells_of(p);
-    k.xchunk = p->fused_xchunk;
-    k.ldE = k.J + 2 * p->sz;
-    k.ldH = k.J + p->sz;
-    // face index per axis/side, for the psi pointers of each step
-    int fidx[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
+    const uint32_t sa[3] = {p->sx, p->sy, p->sz};
+    for (int r = 0; r < 3; ++r) fidx[r][0] = fidx[r][1] = -1;
     for (int f = 0; f < p->d.n_pml; ++f) {
         const FdtdPmlDesc &pd = p->d.pml[f];
-        const uint32_t sa = pd.axis == 0 ? p->sx : pd.axis == 1 ? p->sy : p->sz;
-        FAxis<R> &a = k.ax[pd.axis];
-        if (pd.polarity == 1 && (uint32_t)pd.thickness > sa) continue;  // never applies
+        if (pd.thickness <= 0 || (pd.polarity == 1 && (uint32_t)pd.thickness > sa[pd.axis])) continue;
+        StepAxis<R> &a = k.ax[pd.axis];
         const int side = pd.polarity;
         if (side == 0) a.Tn = pd.thickness;
         else a.Tp = pd.thickness;
@@ -549,7 +504,124 @@ int run_fused(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
         }
         fidx[pd.axis][side] = f;
     }
+}
+
+// Tiling of the one-pass step for a plan: own rows per tile, tiles, x chunk, stages, threads and
+// the stage layout. False when the kernel does not apply (z rows too long, or too little shared
+// memory for two stages).
+template <typename R>
+bool step_layout(const FdtdPlan *p, StepK<R> &k, uint32_t &threads, size_t &smem)
+{
+    constexpr uint32_t V = 16 / sizeof(R);
+    const uint32_t maxr = step_max_rows<R>(p->sz);
+    if (!maxr) return false;
+    uint32_t rows = p->fused_rows ? (p->fused_rows < maxr ? p->fused_rows : maxr) : maxr;
+    if (rows > p->sy) rows = p->sy;
+    k.ntile = (p->sy + rows - 1) / rows;
+    const uint32_t own = (p->sy + k.ntile - 1) / k.ntile;   // most own rows of any tile
+    threads = step_threads(own, p->sz);
+    // stage: the field slots, then the z-face CPML slots sized for own + 3 staged rows
+    const uint32_t nf = p->d.has_mu ? 12u : 9u;
+    uint32_t off = nf * (uint32_t)StepCfg<R>::STR;
+    for (int q = 0; q < SG_NZ; ++q) {
+        const int side = (q >> 1) & 1;
+        const uint32_t T = (uint32_t)(side ? k.ax[2].Tp : k.ax[2].Tn);
+        k.zoff[q] = off;
+        if (T) off += ((own + 3u) * T + 2u * (V - 1u) + V - 1u) / V * V;
+    }
+    k.stage_elems = off;
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
+    uint32_t ns = p->fused_stages ? p->fused_stages : 4u;
+    while (ns >= 2 && step_smem_bytes<R>(ns, k.stage_elems) > (size_t)optin) --ns;
+    if (ns < 2) return false;
+    k.nstage = ns;
+    smem = step_smem_bytes<R>(ns, k.stage_elems);
+    // x chunk: as many chunks as give whole waves of one block per SM
+    uint32_t xc = p->fused_xchunk;
+    if (!xc) {
+        int nsm = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device);
+        if (nsm < 1) nsm = 1;
+        const uint32_t waves = (k.ntile + (uint32_t)nsm - 1) / (uint32_t)nsm;
+        uint32_t nchunk = waves * (uint32_t)nsm / k.ntile;
+        if (nchunk < 1) nchunk = 1;
+        if (nchunk > p->sx) nchunk = p->sx;
+        xc = (p->sx + nchunk - 1) / nchunk;
+    }
+    k.xchunk = xc;
+    return true;
+}
+
+// One-pass multi-step path: one launch per step, reading A and writing B, then swapping; the
+// state is brought home after an odd number of steps.
+template <typename R>
+int run_fused(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
+              const FdtdPointSources *src, const FdtdDftMonitor *mon)
+{
+    StepK<R> k;
+    std::memset(&k, 0, sizeof(k));
+    k.sx = p->sx;
+    k.sy = p->sy;
+    k.sz = p->sz;
+    k.syz = p->syz;
+    k.N = p->N;
+    k.dt = (R)p->d.dt;
+    k.inv_d = (R)(1.0 / p->d.dx);
+    k.sf = (R)((double)k.dt * 0.125);
+    for (int r = 0; r < 3; ++r) {
+        k.inv_de[r] = p->d.uniform ? nullptr : (const R *)b->inv_de[r];
+        k.inv_dh[r] = p->d.uniform ? nullptr : (const R *)b->inv_dh[r];
+    }
+    const int dxmode = !p->d.uniform ? 2 : ((R)(1.0 / p->d.dx) == R(1) ? 0 : 1);
+    const bool mu = p->d.has_mu != 0;
+    k.ce = (const R *)b->ce;
+    k.cm = mu ? (const R *)b->cm : nullptr;
+    k.S = (R *)b->S;
+    k.oS = (R *)b->oS;
+    k.poynt = p->d.do_poynting ? 1 : 0;
+    k.status = p->status;
+    k.wait_ns = 2000000000u;
+    if (src && src->n > 0) {
+        k.nsrc = src->n;
+        k.src_values = (const R *)src->values;
+        for (int s = 0; s < src->n; ++s) {
+            const uint64_t ind = (uint64_t)src->index[s];
+            const uint64_t cell = ind % p->N;
+            k.src_c[s] = (int32_t)(ind / p->N);
+            k.src_x[s] = (uint32_t)(cell / p->syz);
+            k.src_j[s] = (uint32_t)(cell % p->syz);
+        }
+    }
+    int fidx[3][2];
+    step_faces<R>(p, k, fidx);
+    uint32_t threads = 0;
+    size_t smem = 0;
+    if (!step_layout<R>(p, k, threads, smem)) return fail(FDTD_ERR_UNSUPPORTED, "fdtd_run: one-pass step does not fit");
+    for (int c = 0; c < SG_NF; ++c) k.len[c] = 3 * p->N;
+    for (int q = 0; q < SG_NZ; ++q) {
+        const int side = (q >> 1) & 1;
+        k.len[SG_NF + q] = (uint64_t)p->sx * p->sy * (uint64_t)(side ? k.ax[2].Tp : k.ax[2].Tn);
+    }
+    // bulk copies need 16-byte aligned bases for every staged array of both parities
+    bool al = p->fused_tma && aligned16(b->E) && aligned16(b->E2) && aligned16(b->H) && aligned16(b->H2) &&
+              aligned16(b->ce) && (!mu || aligned16(b->cm));
+    for (int side = 0; side < 2 && al; ++side) {
+        const int f = fidx[2][side];
+        if (f < 0) continue;
+        for (int c = 0; c < 2; ++c)
+            al = al && aligned16(b->psi_e[f][c]) && aligned16(b->psi_e2[f][c]) && aligned16(b->psi_h[f][c]) &&
+                 aligned16(b->psi_h2[f][c]);
+    }
+    k.tma = al ? 1 : 0;
+    p->step_cfg[0] = (int32_t)((p->sy + k.ntile - 1) / k.ntile);
+    p->step_cfg[1] = (int32_t)k.xchunk;
+    p->step_cfg[2] = (int32_t)k.nstage;
+    p->step_cfg[3] = (int32_t)threads;
     void *E[2] = {b->E, b->E2}, *H[2] = {b->H, b->H2};
+    KernelTimer timer(p, nsteps, st);
+    int rc;
+    if ((rc = timer.init())) return rc;
     for (int t = 0; t < nsteps; ++t) {
         const int a = t & 1, o = a ^ 1;
         k.EA = (const R *)E[a];
@@ -572,15 +644,19 @@ int run_fused(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
                 }
             }
         k.t = t;
-        k.write_oS = poynt && t == nsteps - 1;
-        int rc = check_cuda(launch_fused<R>(k, p->d.has_mu != 0, poynt, dxmode, st), "fused step launch");
-        if (!rc && mon) rc = run_dft<R>(p, E[o], st, mon, t);
-        if (rc) return rc;
+        k.write_oS = k.poynt && t == nsteps - 1;
+        if ((rc = timer.mark(t, 0))) return rc;
+        if ((rc = check_cuda(launch_step<R>(k, dxmode, mu, threads, smem, st), "one-pass step launch"))) return rc;
+        if ((rc = timer.mark(t, 1))) return rc;
+        if ((rc = timer.mark(t, 2))) return rc;
+        if ((rc = timer.mark(t, 3))) return rc;
+        if (mon && (rc = run_dft<R>(p, E[o], st, mon, t))) return rc;
     }
+    if ((rc = timer.finish())) return rc;
     if (nsteps & 1) {
-        // the last step wrote the scratch copies: bring the state home
+        // the last step wrote the second copies: bring the state home
         const size_t fb = 3 * (size_t)p->N * p->elem;
-        int rc = check_cuda(cudaMemcpyAsync(b->E, b->E2, fb, cudaMemcpyDeviceToDevice, st), "copy E");
+        rc = check_cuda(cudaMemcpyAsync(b->E, b->E2, fb, cudaMemcpyDeviceToDevice, st), "copy E");
         if (!rc) rc = check_cuda(cudaMemcpyAsync(b->H, b->H2, fb, cudaMemcpyDeviceToDevice, st), "copy H");
         for (int f = 0; !rc && f < p->d.n_pml; ++f) {
             const FdtdPmlDesc &pd = p->d.pml[f];
@@ -670,11 +746,20 @@ bool fused_eligible(const FdtdPlan *p, const FdtdBuffers *b, const FdtdPointSour
         if (p->d.pml[f].thickness > 0 &&
             (!b->psi_e2[f][0] || !b->psi_e2[f][1] || !b->psi_h2[f][0] || !b->psi_h2[f][1]))
             return false;
-    if (src && src->n > FUSED_MAX_SRC) return false;
-    const uint32_t J = fused_cells_of(p);
-    if (J == 0) return false;
-    const size_t smem = (6 * (size_t)(J + 2 * p->sz) + 6 * (size_t)(J + p->sz)) * p->elem;
-    return smem <= 200 * 1024;
+    if (src && src->n > STEP_MAX_SRC) return false;
+    uint32_t threads = 0;
+    size_t smem = 0;
+    int fidx[3][2];
+    if (p->d.dtype == FDTD_F64) {
+        StepK<double> k;
+        std::memset(&k, 0, sizeof(k));
+        step_faces<double>(p, k, fidx);
+        return step_layout<double>(p, k, threads, smem);
+    }
+    StepK<float> k;
+    std::memset(&k, 0, sizeof(k));
+    step_faces<float>(p, k, fidx);
+    return step_layout<float>(p, k, threads, smem);
 }
 
 // The H+S path: Poynting on, no Bloch boundaries, CPML faces of one axis disjoint, dt/eps
@@ -726,20 +811,34 @@ int fdtd_plan_create(const FdtdDesc *desc, FdtdPlan **out)
     // Whole-grid launches measured fastest on GB300 for the 395x345x73 workload (0.33 ms per
     // step against 0.43-0.86 ms for 48- to 8-plane slabs), so slabs are opt-in.
     p->slab = 0;
-    p->fused_cells = 0;
+    p->fused_rows = 0;
+    p->fused_stages = 0;
+    p->fused_tma = 1;
+    p->last_run_path = FDTD_PATH_NONE;
+    std::memset(p->step_cfg, 0, sizeof(p->step_cfg));
     p->hs_xchunk = 16;
     p->hs_prefetch = 0;
     p->timing = 0;
     p->kernel_ms[0] = p->kernel_ms[1] = 0.0;
     p->kernel_samples = 0;
-    p->fused_xchunk = 16;
+    p->fused_xchunk = 0;
     cudaGetDevice(&p->device);
+    {
+        cudaError_t e = cudaMalloc(&p->status, sizeof(int32_t));
+        if (e == cudaSuccess) e = cudaMemset(p->status, 0, sizeof(int32_t));
+        if (e != cudaSuccess) {
+            if (p->status) cudaFree(p->status);
+            delete p;
+            return cuda_fail(e, "cudaMalloc(status word)");
+        }
+    }
     size_t total = 0;
     for (int f = 0; f < desc->n_pml; ++f) total += 6 * (size_t)desc->pml[f].thickness;
     std::memset(p->tab, 0, sizeof(p->tab));
     if (total) {
         cudaError_t e = cudaMalloc(&p->coef, total * p->elem);
         if (e != cudaSuccess) {
+            cudaFree(p->status);
             delete p;
             return cuda_fail(e, "cudaMalloc(coefficient tables)");
         }
@@ -758,6 +857,7 @@ int fdtd_plan_create(const FdtdDesc *desc, FdtdPlan **out)
         e = cudaMemcpy(p->coef, host.data(), host.size(), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) {
             cudaFree(p->coef);
+            cudaFree(p->status);
             delete p;
             return cuda_fail(e, "cudaMemcpy(coefficient tables)");
         }
@@ -771,6 +871,7 @@ int fdtd_plan_destroy(FdtdPlan *plan)
 {
     if (!plan) return FDTD_OK;
     if (plan->coef) cudaFree(plan->coef);
+    if (plan->status) cudaFree(plan->status);
     delete plan;
     return FDTD_OK;
 }
@@ -787,14 +888,22 @@ int fdtd_plan_tune(FdtdPlan *p, int32_t key, int32_t value)
         if (value < 0) return fail(FDTD_ERR_INVALID, "slab must be >= 0 (0: whole grid)");
         p->slab = (uint32_t)value;
         return FDTD_OK;
-    case FDTD_TUNE_FUSED_CELLS:
-        if (value < 0 || value > 8192 || (value % 32))
-            return fail(FDTD_ERR_INVALID, "fused_cells must be 0 or a multiple of 32 up to 8192");
-        p->fused_cells = (uint32_t)value;
+    case FDTD_TUNE_FUSED_ROWS:
+        if (value < 0 || value > 1024) return fail(FDTD_ERR_INVALID, "fused_rows must be in [0, 1024]");
+        p->fused_rows = (uint32_t)value;
         return FDTD_OK;
     case FDTD_TUNE_FUSED_XCHUNK:
-        if (value < 1 || value > 4096) return fail(FDTD_ERR_INVALID, "fused_xchunk must be in [1, 4096]");
+        if (value < 0 || value > 65536) return fail(FDTD_ERR_INVALID, "fused_xchunk must be in [0, 65536]");
         p->fused_xchunk = (uint32_t)value;
+        return FDTD_OK;
+    case FDTD_TUNE_FUSED_STAGES:
+        if (value != 0 && (value < 2 || value > STEP_MAX_STAGES))
+            return fail(FDTD_ERR_INVALID, "fused_stages must be 0 or in [2, 6]");
+        p->fused_stages = (uint32_t)value;
+        return FDTD_OK;
+    case FDTD_TUNE_FUSED_TMA:
+        if (value != 0 && value != 1) return fail(FDTD_ERR_INVALID, "fused_tma must be 0 or 1");
+        p->fused_tma = value;
         return FDTD_OK;
     case FDTD_TUNE_HS_XCHUNK:
         if (value < 1 || value > 4096) return fail(FDTD_ERR_INVALID, "hs_xchunk must be in [1, 4096]");
@@ -819,8 +928,15 @@ int fdtd_plan_get(const FdtdPlan *p, int32_t key, int32_t *value)
     switch (key) {
     case FDTD_TUNE_XCHUNK: *value = p->xchunk; return FDTD_OK;
     case FDTD_TUNE_SLAB: *value = (int32_t)p->slab; return FDTD_OK;
-    case FDTD_TUNE_FUSED_CELLS: *value = (int32_t)p->fused_cells; return FDTD_OK;
+    case FDTD_TUNE_FUSED_ROWS: *value = (int32_t)p->fused_rows; return FDTD_OK;
     case FDTD_TUNE_FUSED_XCHUNK: *value = (int32_t)p->fused_xchunk; return FDTD_OK;
+    case FDTD_TUNE_FUSED_STAGES: *value = (int32_t)p->fused_stages; return FDTD_OK;
+    case FDTD_TUNE_FUSED_TMA: *value = p->fused_tma; return FDTD_OK;
+    case FDTD_GET_LAST_RUN_PATH: *value = p->last_run_path; return FDTD_OK;
+    case FDTD_GET_STEP_ROWS: *value = p->step_cfg[0]; return FDTD_OK;
+    case FDTD_GET_STEP_XCHUNK: *value = p->step_cfg[1]; return FDTD_OK;
+    case FDTD_GET_STEP_STAGES: *value = p->step_cfg[2]; return FDTD_OK;
+    case FDTD_GET_STEP_THREADS: *value = p->step_cfg[3]; return FDTD_OK;
     case FDTD_TUNE_HS_XCHUNK: *value = (int32_t)p->hs_xchunk; return FDTD_OK;
     case FDTD_TUNE_HS_PREFETCH: *value = p->hs_prefetch; return FDTD_OK;
     case FDTD_TUNE_TIMING: *value = p->timing; return FDTD_OK;
@@ -1066,6 +1182,7 @@ int fdtd_run(FdtdPlan *p, const FdtdBuffers *b, void *stream, int32_t nsteps,
     if (!b->E2 && hs_eligible(p, b)) {
         if ((rc = check_run_buffers(p, b))) return rc;
         cudaStream_t st = (cudaStream_t)stream;
+        p->last_run_path = FDTD_PATH_HS;
         rc = f64 ? run_hs<double>(p, b, st, nsteps, src, mon) : run_hs<float>(p, b, st, nsteps, src, mon);
         if (!rc && mon) { mon->step += nsteps; mon->series_row += nsteps; }
         return rc;
@@ -1074,6 +1191,7 @@ int fdtd_run(FdtdPlan *p, const FdtdBuffers *b, void *stream, int32_t nsteps,
         if ((rc = check_psi(p, b->psi_e, "fdtd_run")) || (rc = check_psi(p, b->psi_h, "fdtd_run")))
             return rc;
         cudaStream_t st = (cudaStream_t)stream;
+        p->last_run_path = FDTD_PATH_ONEPASS;
         rc = f64 ? run_fused<double>(p, b, st, nsteps, src, mon) : run_fused<float>(p, b, st, nsteps, src, mon);
         if (!rc && mon) { mon->step += nsteps; mon->series_row += nsteps; }
         return rc;
@@ -1081,9 +1199,25 @@ int fdtd_run(FdtdPlan *p, const FdtdBuffers *b, void *stream, int32_t nsteps,
     // validate once with the per-update entry points' checks, then run the slab schedule
     if ((rc = check_run_buffers(p, b))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
+    p->last_run_path = FDTD_PATH_PER_UPDATE;
     rc = f64 ? run_slabs<double>(p, b, st, nsteps, src, mon) : run_slabs<float>(p, b, st, nsteps, src, mon);
     if (!rc && mon) { mon->step += nsteps; mon->series_row += nsteps; }
     return rc;
+}
+
+int fdtd_device_status(FdtdPlan *p, void *stream, int32_t *bits)
+{
+    if (!p || !bits) return fail(FDTD_ERR_INVALID, "fdtd_device_status: NULL pointer");
+    cudaStream_t st = (cudaStream_t)stream;
+    int32_t v = 0;
+    int rc = check_cuda(cudaMemcpyAsync(&v, p->status, sizeof(v), cudaMemcpyDeviceToHost, st), "status read");
+    if (!rc) rc = check_cuda(cudaMemsetAsync(p->status, 0, sizeof(v), st), "status clear");
+    if (!rc) rc = check_cuda(cudaStreamSynchronize(st), "status sync");
+    if (rc) return rc;
+    *bits = v;
+    if (v)
+        return fail(FDTD_ERR_WATCHDOG, "a bounded wait inside a kernel ran out (status bits " + std::to_string(v) + ")");
+    return FDTD_OK;
 }
 
 int fdtd_run_kernel_ms(const FdtdPlan *p, double ms[2], int32_t *samples)

@@ -14,11 +14,16 @@ struct FdtdPlan {
     int device;                 // device that was current at creation
     int32_t xchunk;             // x planes a bulk-kernel thread marches
     uint32_t slab;              // x planes per L2-resident slab in fdtd_run (0: whole grid)
-    uint32_t fused_cells;       // plane cells one block of the fused step owns
-    uint32_t fused_xchunk;      // x planes one block of the fused step marches
+    uint32_t fused_rows;        // own rows of a one-pass step tile (0: the most that fit)
+    uint32_t fused_xchunk;      // x planes one block of the one-pass step marches (0: automatic)
+    uint32_t fused_stages;      // stages of the one-pass step's ring (0: 4, or as many as fit)
+    int32_t fused_tma;          // one-pass step stages non-wrapping tiles by bulk copies
+    int32_t last_run_path;      // FDTD_PATH_* of the last fdtd_run
+    int32_t step_cfg[4];        // last one-pass launch: rows, xchunk, stages, threads
     uint32_t hs_xchunk;         // x planes one block of the H+S kernel marches
     int32_t hs_prefetch;        // H+S kernel issues the next plane's loads early
     int32_t timing;             // fdtd_run's H+S path records per-kernel CUDA events
+    int32_t *status = nullptr;  // device word: bits of bounded waits inside kernels that ran out
     double kernel_ms[2];        // last timed run: mean update_E and H+S launch times (ms)
     int32_t kernel_samples;     // launches each mean is over
     void *coef = nullptr;       // device copy of every face's six coefficient tables

@@ -481,7 +481,8 @@ class Simulation:
                    CPML arrays) from one copy and writing a second: 96 B per cell per step;
           'plain'  the per-update kernels (E, H, S), optionally over L2-resident x slabs
                    (tune(slab=...));
-          'fused'  E, sources, H and S in one kernel per step (no Bloch boundaries).
+          'fused'  E, sources, H and S in one kernel per step (no Bloch boundaries), reading
+                   every field once and writing it once: 72 B per cell per step.
         The 'hs' and 'fused' paths write oS on the last step only."""
         nsteps = int(nsteps)
         if watchdog and int(watchdog) > 0:
@@ -615,16 +616,43 @@ class Simulation:
         _lib.check(self._lib.fdtd_plan_get(self._plan, _lib.FDTD_TUNE_SLAB, ctypes.byref(v)))
         return v.value or self.shape[0]
 
-    def tune(self, xchunk: int = None, slab: int = None, fused_cells: int = None,
-             fused_xchunk: int = None, hs_xchunk: int = None, hs_prefetch: bool = None):
-        """Kernel tiling (None keeps a value); results do not depend on it."""
+    def tune(self, xchunk: int = None, slab: int = None, fused_rows: int = None,
+             fused_xchunk: int = None, hs_xchunk: int = None, hs_prefetch: bool = None,
+             fused_stages: int = None, fused_tma: bool = None):
+        """Kernel tiling (None keeps a value); results do not depend on it.
+
+        fused_rows / fused_xchunk / fused_stages: own y rows of a one-pass step tile, x planes
+        of a block, planes in its shared-memory ring (0: automatic); fused_tma: stage the rows
+        of non-wrapping tiles with bulk asynchronous copies (default) or per element."""
         for key, val in ((_lib.FDTD_TUNE_XCHUNK, xchunk), (_lib.FDTD_TUNE_SLAB, slab),
-                         (_lib.FDTD_TUNE_FUSED_CELLS, fused_cells),
+                         (_lib.FDTD_TUNE_FUSED_ROWS, fused_rows),
                          (_lib.FDTD_TUNE_FUSED_XCHUNK, fused_xchunk),
                          (_lib.FDTD_TUNE_HS_XCHUNK, hs_xchunk),
-                         (_lib.FDTD_TUNE_HS_PREFETCH, None if hs_prefetch is None else int(hs_prefetch))):
+                         (_lib.FDTD_TUNE_HS_PREFETCH, None if hs_prefetch is None else int(hs_prefetch)),
+                         (_lib.FDTD_TUNE_FUSED_STAGES, fused_stages),
+                         (_lib.FDTD_TUNE_FUSED_TMA, None if fused_tma is None else int(fused_tma))):
             if val is not None:
                 _lib.check(self._lib.fdtd_plan_tune(self._plan, key, int(val)))
+
+    def tuning(self, key: str) -> int:
+        """Current value of a tuning key ('fused_rows', 'hs_xchunk', ...) or of a read-only key:
+        'last_run_path' (0 none, 1 per-update, 2 H+S, 3 one-pass) and 'step_rows',
+        'step_xchunk', 'step_stages', 'step_threads' (tiling of the last one-pass launch)."""
+        name = key.upper()
+        const = getattr(_lib, "FDTD_GET_" + name, None)
+        if const is None:
+            const = getattr(_lib, "FDTD_TUNE_" + name)
+        v = ctypes.c_int32()
+        _lib.check(self._lib.fdtd_plan_get(self._plan, const, ctypes.byref(v)))
+        return v.value
+
+    def device_status(self) -> int:
+        """Bits of bounded device-side waits that ran out since the last call (0: none); waits
+        for the queue. Raises FdtdError (FDTD_ERR_WATCHDOG) when any bit is set."""
+        bits = ctypes.c_int32()
+        _lib.check(self._lib.fdtd_device_status(self._plan, ctypes.c_void_p(self.queue.cuda_stream),
+                                                ctypes.byref(bits)))
+        return bits.value
 
     def get(self, name: str) -> numpy.ndarray:
         """Host copy of a field (what ``pyopencl.array.Array.get()`` returns)."""

@@ -1,6 +1,8 @@
-"""The fused multi-step kernel (Simulation.run with fused=True) against the per-call drop-in
-loop and the oracle: bit-identical E, H, S and CPML state for every tiling, including tiles
-so small that the halo and wrap-around recomputation paths run."""
+"""The one-pass step kernel (Simulation.run(path='fused')) against the per-call drop-in loop and
+the oracle: bit-identical E, H, S and CPML state for every tiling (rows per tile, x chunk, stage
+count), with the rows of non-wrapping tiles staged by bulk copies or by per-element copies,
+including tiles of one row, chunks of one plane and z faces whose thickness is not a multiple
+of the 16-byte unit."""
 import copy
 import math
 import os
@@ -43,20 +45,61 @@ def _same_state(a, b, poynting):
             assert torch.equal(u1, u2) and torch.equal(v1, v2), fld
 
 
+# (rows per tile, x chunk, stages, bulk copies)
+TILINGS = [(0, 0, 0, 1), (1, 3, 2, 1), (2, 1, 3, 0), (3, 2, 0, 1), (5, 7, 2, 0), (4, 5, 4, 1)]
+
+
+def _tune(sim, tiling):
+    rows, xc, ns, tma = tiling
+    sim.tune(fused_rows=rows, fused_xchunk=xc, fused_stages=ns, fused_tma=bool(tma))
+
+
 @pytest.mark.parametrize("name", ["c1_small", "pml_mixed", "periodic_pec_poynting", "nonuniform",
                                   "dx_half", "f64_mixed"])
-@pytest.mark.parametrize("tiles", [(0, 0), (32, 3), (64, 1), (96, 2)])
+@pytest.mark.parametrize("tiling", TILINGS)
 @pytest.mark.parametrize("nsteps", [7, 10])
-def test_fused_equals_per_call_loop(name, tiles, nsteps):
+def test_fused_equals_per_call_loop(name, tiling, nsteps):
     kw, loop = cases.build(name)
     src = _sources(kw, loop, nsteps)
     a = _gpu(**copy.deepcopy(kw))
     b = _gpu(**copy.deepcopy(kw))
-    if tiles[0]:
-        b.tune(fused_cells=tiles[0], fused_xchunk=tiles[1])
+    _tune(b, tiling)
     a.run(nsteps, point_sources=src, path="plain")
     b.run(nsteps, point_sources=src, path="fused")
+    assert b.tuning("last_run_path") == 3
+    assert b.device_status() == 0
     _same_state(a, b, kw.get("do_poynting", True))
+
+
+@pytest.mark.parametrize("shape,faces,T", [((9, 40, 37), "xyz", (3, 5, 6)), ((6, 23, 18), "yz", (2, 4, 7)),
+                                           ((7, 31, 20), "z", (0, 0, 9)), ((5, 17, 11), "", (0, 0, 0))])
+@pytest.mark.parametrize("tiling", [(1, 2, 2, 1), (3, 4, 3, 1), (6, 0, 0, 1), (2, 3, 4, 0)])
+@pytest.mark.parametrize("dtype,mu", [(numpy.float32, False), (numpy.float32, True), (numpy.float64, True)])
+def test_fused_many_tiles(shape, faces, T, tiling, dtype, mu):
+    """Grids with many tiles, most of them staged by bulk copies, CPML faces of uneven
+    thickness (the 'p' side one cell thinner), a PEC row, mu and two point sources."""
+    rng = numpy.random.default_rng(sum(shape) + 7 * len(faces))
+    eps = [rng.uniform(1, 5, shape).astype(dtype) for _ in range(3)]
+    eps[1][shape[0] // 2, shape[1] // 3, :3] = numpy.inf
+    kw = dict(epsilon=eps, do_poynting=True,
+              pmls=[{"axis": a, "polarity": p, "thickness": max(1, T["xyz".index(a)] - (p == "p"))}
+                    for a in faces for p in "np"],
+              initial_fields={k: [rng.standard_normal(shape).astype(dtype) for _ in range(3)] for k in "EH"})
+    if mu:
+        kw["mu"] = [rng.uniform(1, 2, shape).astype(dtype) for _ in range(3)]
+    N = int(numpy.prod(shape))
+    steps = 9
+    srcs = [(int(numpy.ravel_multi_index((shape[0] // 2, 1, shape[2] - 1), shape)) + 2 * N,
+             [math.sin(0.4 * t) for t in range(steps)]),
+            (int(numpy.ravel_multi_index((0, shape[1] - 2, 0), shape)) + 1 * N, [0.25] * steps)]
+    a = _gpu(**copy.deepcopy(kw))
+    b = _gpu(**copy.deepcopy(kw))
+    _tune(b, tiling)
+    a.run(steps, point_sources=srcs, path="plain")
+    b.run(steps, point_sources=srcs, path="fused")
+    assert b.tuning("last_run_path") == 3
+    assert b.device_status() == 0
+    _same_state(a, b, True)
 
 
 def test_fused_matches_oracle_with_mu_and_sources():
@@ -70,8 +113,9 @@ def test_fused_matches_oracle_with_mu_and_sources():
             (int(numpy.ravel_multi_index((9, 8, 10), shape)) + 2 * N, [0.5] * steps)]
     kw = dict(epsilon=eps, mu=mu, pmls=pmls, do_poynting=True)
     g = _gpu(**copy.deepcopy(kw))
-    g.tune(fused_cells=64, fused_xchunk=4)
+    g.tune(fused_rows=3, fused_xchunk=4)
     g.run(steps, point_sources=srcs, path="fused")
+    assert g.tuning("last_run_path") == 3
     c = port.PortSimulation(nthreads=os.cpu_count(), **copy.deepcopy(kw))
     for t in range(steps):
         c.update_E()
