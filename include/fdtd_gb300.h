@@ -131,9 +131,14 @@ int fdtd_plan_destroy(FdtdPlan *plan);
  *   FUSED_TMA     1 (default): the one-pass step stages the rows of tiles that do not wrap around
  *                 the y boundary with bulk asynchronous copies when every staged buffer is
  *                 16-byte aligned; 0: per-element asynchronous copies everywhere
+ *   FUSED_SHAPE   block shape of the one-pass step: 1 large (up to 1024 threads, one block per
+ *                 SM), 2 small (up to 512 threads, two blocks per SM; float32 only), 0
+ *                 (default) small when its tiles hold at least 3 own rows
  *   HS_XCHUNK     x planes one block of the H+S kernel of fdtd_run marches (default 16)
  *   HS_PREFETCH   1: the H+S kernel loads the next plane ahead (one block per SM); 0: not
  *                 (two blocks per SM, the default)
+ *   HS_REVERSE    1 (default): the H+S kernel takes its x chunks in descending order, so that it
+ *                 starts on the planes update_E wrote last (still in L2); 0: ascending
  *   TIMING        1: fdtd_run records CUDA events around its kernels on up to 64 steps spread
  *                 over the call (update_E and H+S on the H+S path, the step kernel on the
  *                 one-pass path) and waits for the stream before it returns (profiling; read
@@ -147,13 +152,16 @@ int fdtd_plan_destroy(FdtdPlan *plan);
 #define FDTD_TUNE_TIMING 7
 #define FDTD_TUNE_FUSED_STAGES 8
 #define FDTD_TUNE_FUSED_TMA 9
+#define FDTD_TUNE_FUSED_SHAPE 10
+#define FDTD_TUNE_HS_REVERSE 11
 /* Read-only keys of fdtd_plan_get: the path of the last fdtd_run (FDTD_PATH_*) and the tiling
- * of its last one-pass launch (own rows per tile, x chunk, stages, threads per block). */
+ * of its last one-pass launch (own rows per tile, x chunk, stages, threads per block, shape). */
 #define FDTD_GET_LAST_RUN_PATH 100
 #define FDTD_GET_STEP_ROWS 101
 #define FDTD_GET_STEP_XCHUNK 102
 #define FDTD_GET_STEP_STAGES 103
 #define FDTD_GET_STEP_THREADS 104
+#define FDTD_GET_STEP_SHAPE 105
 #define FDTD_PATH_NONE 0
 #define FDTD_PATH_PER_UPDATE 1     /* update_E, sources, update_H, update_S launches */
 #define FDTD_PATH_HS 2             /* update_E in place, sources, H and S in one launch */

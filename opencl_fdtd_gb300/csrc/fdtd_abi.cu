@@ -366,6 +366,7 @@ int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
     k.oS = (R *)b->oS;
     k.dsz = FastDiv::make(p->sz);
     k.rows = (uint32_t)HS_THREADS / p->sz - 1u;
+    k.reverse = p->hs_reverse;
     k.xchunk = p->hs_xchunk;
     int fidx[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
     for (int f = 0; f < p->d.n_pml; ++f) {
@@ -484,67 +485,88 @@ int run_slabs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
 // ---- one-pass step (step_kernel.cu) -------------------------------------------------------
 bool aligned16(const void *q) { return ((uintptr_t)q & 15u) == 0; }
 
-// CPML faces of the one-pass step (a 'p' face thicker than its axis never applies) and the plan's
-// face index per axis and side (-1: none).
+// CPML faces of the one-pass step (a 'p' face thicker than its axis never applies), the offset
+// of each face's six coefficient tables in the plan's table block, and the plan's face index per
+// axis and side (-1: none).
 template <typename R>
 void step_faces(const FdtdPlan *p, StepK<R> &k, int fidx[3][2])
 {
     const uint32_t sa[3] = {p->sx, p->sy, p->sz};
     for (int r = 0; r < 3; ++r) fidx[r][0] = fidx[r][1] = -1;
+    size_t off = 0;
     for (int f = 0; f < p->d.n_pml; ++f) {
         const FdtdPmlDesc &pd = p->d.pml[f];
+        const size_t here = off;
+        off += 6 * (size_t)(pd.thickness > 0 ? pd.thickness : 0);
         if (pd.thickness <= 0 || (pd.polarity == 1 && (uint32_t)pd.thickness > sa[pd.axis])) continue;
         StepAxis<R> &a = k.ax[pd.axis];
         const int side = pd.polarity;
         if (side == 0) a.Tn = pd.thickness;
         else a.Tp = pd.thickness;
-        for (int c = 0; c < 3; ++c) {
-            a.tab[0][side][c] = (const R *)p->tab[f][c];
-            a.tab[1][side][c] = (const R *)p->tab[f][3 + c];
-        }
+        k.coff[pd.axis][side] = (int32_t)here;
         fidx[pd.axis][side] = f;
     }
+    k.coef = (const R *)p->coef;
+    k.ncoef = (uint32_t)off;
 }
 
-// Tiling of the one-pass step for a plan: own rows per tile, tiles, x chunk, stages, threads and
-// the stage layout. False when the kernel does not apply (z rows too long, or too little shared
-// memory for two stages).
+// Tiling of the one-pass step for a plan: block shape, own rows per tile, tiles, x chunk, stages,
+// threads and the stage layout. False when the kernel does not apply (z rows too long, too many
+// CPML coefficients, or too little shared memory for two stages).
 template <typename R>
-bool step_layout(const FdtdPlan *p, StepK<R> &k, uint32_t &threads, size_t &smem)
+bool step_layout(const FdtdPlan *p, StepK<R> &k, int &shape, uint32_t &threads, size_t &smem)
 {
     constexpr uint32_t V = 16 / sizeof(R);
-    const uint32_t maxr = step_max_rows<R>(p->sz);
+    if (k.ncoef > (uint32_t)STEP_MAX_COEF) return false;
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
+    int smsm = 0;
+    cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, p->device);
+    // block shape: the two-blocks-per-SM shape when a tile of it holds at least 3 own rows
+    shape = STEP_SHAPE_BIG;
+    if (sizeof(R) == 4) {
+        if (p->fused_shape == STEP_SHAPE_SMALL) shape = STEP_SHAPE_SMALL;
+        else if (!p->fused_shape && step_max_rows<R>(STEP_SHAPE_SMALL, p->sz) >= 3) shape = STEP_SHAPE_SMALL;
+    }
+    const uint32_t maxr = step_max_rows<R>(shape, p->sz);
     if (!maxr) return false;
     uint32_t rows = p->fused_rows ? (p->fused_rows < maxr ? p->fused_rows : maxr) : maxr;
     if (rows > p->sy) rows = p->sy;
     k.ntile = (p->sy + rows - 1) / rows;
     const uint32_t own = (p->sy + k.ntile - 1) / k.ntile;   // most own rows of any tile
     threads = step_threads(own, p->sz);
-    // stage: the field slots, then the z-face CPML slots sized for own + 3 staged rows
+    // stage: the field slots, then the z-face CPML slots (four per side) for own + 3 staged rows
     const uint32_t nf = p->d.has_mu ? 12u : 9u;
-    uint32_t off = nf * (uint32_t)StepCfg<R>::STR;
-    for (int q = 0; q < SG_NZ; ++q) {
-        const int side = (q >> 1) & 1;
+    const uint32_t str = sizeof(R) == 8 ? (uint32_t)StepF64::STR
+                       : shape == STEP_SHAPE_SMALL ? (uint32_t)StepSmall::STR : (uint32_t)StepBig::STR;
+    uint32_t off = nf * str;
+    for (int side = 0; side < 2; ++side) {
         const uint32_t T = (uint32_t)(side ? k.ax[2].Tp : k.ax[2].Tn);
-        k.zoff[q] = off;
-        if (T) off += ((own + 3u) * T + 2u * (V - 1u) + V - 1u) / V * V;
+        k.zoff[side] = off;
+        k.zsz[side] = T ? ((own + 3u) * T + 2u * (V - 1u) + V - 1u) / V * V : 0u;
+        off += 4u * k.zsz[side];
     }
     k.stage_elems = off;
-    int optin = 0;
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
+    // shared memory per block: all of it for the large shape, half an SM for the small one
+    size_t cap = (size_t)optin;
+    if (shape == STEP_SHAPE_SMALL) {
+        const size_t half = (size_t)smsm / 2 - 1024;
+        if (half < cap) cap = half;
+    }
     uint32_t ns = p->fused_stages ? p->fused_stages : 4u;
-    while (ns >= 2 && step_smem_bytes<R>(ns, k.stage_elems) > (size_t)optin) --ns;
+    while (ns >= 2 && step_smem_bytes<R>(shape, ns, k.stage_elems, k.ncoef) > cap) --ns;
     if (ns < 2) return false;
     k.nstage = ns;
-    smem = step_smem_bytes<R>(ns, k.stage_elems);
-    // x chunk: as many chunks as give whole waves of one block per SM
+    smem = step_smem_bytes<R>(shape, ns, k.stage_elems, k.ncoef);
+    // x chunk: as many chunks as give whole waves of the resident blocks
     uint32_t xc = p->fused_xchunk;
     if (!xc) {
         int nsm = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device);
         if (nsm < 1) nsm = 1;
-        const uint32_t waves = (k.ntile + (uint32_t)nsm - 1) / (uint32_t)nsm;
-        uint32_t nchunk = waves * (uint32_t)nsm / k.ntile;
+        const uint32_t slots = (uint32_t)nsm * (shape == STEP_SHAPE_SMALL ? 2u : 1u);
+        const uint32_t waves = (k.ntile + slots - 1) / slots;
+        uint32_t nchunk = waves * slots / k.ntile;
         if (nchunk < 1) nchunk = 1;
         if (nchunk > p->sx) nchunk = p->sx;
         xc = (p->sx + nchunk - 1) / nchunk;
@@ -597,10 +619,12 @@ int run_fused(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
     step_faces<R>(p, k, fidx);
     uint32_t threads = 0;
     size_t smem = 0;
-    if (!step_layout<R>(p, k, threads, smem)) return fail(FDTD_ERR_UNSUPPORTED, "fdtd_run: one-pass step does not fit");
+    int shape = 0;
+    if (!step_layout<R>(p, k, shape, threads, smem))
+        return fail(FDTD_ERR_UNSUPPORTED, "fdtd_run: one-pass step does not fit");
     for (int c = 0; c < SG_NF; ++c) k.len[c] = 3 * p->N;
     for (int q = 0; q < SG_NZ; ++q) {
-        const int side = (q >> 1) & 1;
+        const int side = q >> 2;
         k.len[SG_NF + q] = (uint64_t)p->sx * p->sy * (uint64_t)(side ? k.ax[2].Tp : k.ax[2].Tn);
     }
     // bulk copies need 16-byte aligned bases for every staged array of both parities
@@ -618,6 +642,7 @@ int run_fused(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
     p->step_cfg[1] = (int32_t)k.xchunk;
     p->step_cfg[2] = (int32_t)k.nstage;
     p->step_cfg[3] = (int32_t)threads;
+    p->step_cfg[4] = shape;
     void *E[2] = {b->E, b->E2}, *H[2] = {b->H, b->H2};
     KernelTimer timer(p, nsteps, st);
     int rc;
@@ -646,7 +671,7 @@ int run_fused(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
         k.t = t;
         k.write_oS = k.poynt && t == nsteps - 1;
         if ((rc = timer.mark(t, 0))) return rc;
-        if ((rc = check_cuda(launch_step<R>(k, dxmode, mu, threads, smem, st), "one-pass step launch"))) return rc;
+        if ((rc = check_cuda(launch_step<R>(k, shape, dxmode, mu, threads, smem, st), "one-pass step launch"))) return rc;
         if ((rc = timer.mark(t, 1))) return rc;
         if ((rc = timer.mark(t, 2))) return rc;
         if ((rc = timer.mark(t, 3))) return rc;
@@ -749,17 +774,17 @@ bool fused_eligible(const FdtdPlan *p, const FdtdBuffers *b, const FdtdPointSour
     if (src && src->n > STEP_MAX_SRC) return false;
     uint32_t threads = 0;
     size_t smem = 0;
-    int fidx[3][2];
+    int fidx[3][2], shape = 0;
     if (p->d.dtype == FDTD_F64) {
         StepK<double> k;
         std::memset(&k, 0, sizeof(k));
         step_faces<double>(p, k, fidx);
-        return step_layout<double>(p, k, threads, smem);
+        return step_layout<double>(p, k, shape, threads, smem);
     }
     StepK<float> k;
     std::memset(&k, 0, sizeof(k));
     step_faces<float>(p, k, fidx);
-    return step_layout<float>(p, k, threads, smem);
+    return step_layout<float>(p, k, shape, threads, smem);
 }
 
 // The H+S path: Poynting on, no Bloch boundaries, CPML faces of one axis disjoint, dt/eps
@@ -814,10 +839,12 @@ int fdtd_plan_create(const FdtdDesc *desc, FdtdPlan **out)
     p->fused_rows = 0;
     p->fused_stages = 0;
     p->fused_tma = 1;
+    p->fused_shape = 0;
     p->last_run_path = FDTD_PATH_NONE;
     std::memset(p->step_cfg, 0, sizeof(p->step_cfg));
     p->hs_xchunk = 16;
     p->hs_prefetch = 0;
+    p->hs_reverse = 1;
     p->timing = 0;
     p->kernel_ms[0] = p->kernel_ms[1] = 0.0;
     p->kernel_samples = 0;
@@ -905,6 +932,14 @@ int fdtd_plan_tune(FdtdPlan *p, int32_t key, int32_t value)
         if (value != 0 && value != 1) return fail(FDTD_ERR_INVALID, "fused_tma must be 0 or 1");
         p->fused_tma = value;
         return FDTD_OK;
+    case FDTD_TUNE_HS_REVERSE:
+        if (value != 0 && value != 1) return fail(FDTD_ERR_INVALID, "hs_reverse must be 0 or 1");
+        p->hs_reverse = value;
+        return FDTD_OK;
+    case FDTD_TUNE_FUSED_SHAPE:
+        if (value < 0 || value > 2) return fail(FDTD_ERR_INVALID, "fused_shape must be 0, 1 or 2");
+        p->fused_shape = value;
+        return FDTD_OK;
     case FDTD_TUNE_HS_XCHUNK:
         if (value < 1 || value > 4096) return fail(FDTD_ERR_INVALID, "hs_xchunk must be in [1, 4096]");
         p->hs_xchunk = (uint32_t)value;
@@ -932,6 +967,9 @@ int fdtd_plan_get(const FdtdPlan *p, int32_t key, int32_t *value)
     case FDTD_TUNE_FUSED_XCHUNK: *value = (int32_t)p->fused_xchunk; return FDTD_OK;
     case FDTD_TUNE_FUSED_STAGES: *value = (int32_t)p->fused_stages; return FDTD_OK;
     case FDTD_TUNE_FUSED_TMA: *value = p->fused_tma; return FDTD_OK;
+    case FDTD_TUNE_FUSED_SHAPE: *value = p->fused_shape; return FDTD_OK;
+    case FDTD_TUNE_HS_REVERSE: *value = p->hs_reverse; return FDTD_OK;
+    case FDTD_GET_STEP_SHAPE: *value = p->step_cfg[4]; return FDTD_OK;
     case FDTD_GET_LAST_RUN_PATH: *value = p->last_run_path; return FDTD_OK;
     case FDTD_GET_STEP_ROWS: *value = p->step_cfg[0]; return FDTD_OK;
     case FDTD_GET_STEP_XCHUNK: *value = p->step_cfg[1]; return FDTD_OK;

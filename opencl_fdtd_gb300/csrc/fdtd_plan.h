@@ -18,10 +18,12 @@ struct FdtdPlan {
     uint32_t fused_xchunk;      // x planes one block of the one-pass step marches (0: automatic)
     uint32_t fused_stages;      // stages of the one-pass step's ring (0: 4, or as many as fit)
     int32_t fused_tma;          // one-pass step stages non-wrapping tiles by bulk copies
+    int32_t fused_shape;        // one-pass block shape: 0 automatic, 1 large, 2 small
     int32_t last_run_path;      // FDTD_PATH_* of the last fdtd_run
-    int32_t step_cfg[4];        // last one-pass launch: rows, xchunk, stages, threads
+    int32_t step_cfg[5];        // last one-pass launch: rows, xchunk, stages, threads, shape
     uint32_t hs_xchunk;         // x planes one block of the H+S kernel marches
     int32_t hs_prefetch;        // H+S kernel issues the next plane's loads early
+    int32_t hs_reverse;         // H+S kernel takes its x chunks in descending order
     int32_t timing;             // fdtd_run's H+S path records per-kernel CUDA events
     int32_t *status = nullptr;  // device word: bits of bounded waits inside kernels that ran out
     double kernel_ms[2];        // last timed run: mean update_E and H+S launch times (ms)

@@ -213,7 +213,9 @@ __global__ void __launch_bounds__(HS_THREADS, PF ? 1 : 2) k_bulk_hs(const HSK<R>
     const uint32_t y = w ? y0 + w - 1u : (y0 ? y0 - 1u : sy - 1u);
     const bool own = act && w > 0;
     const uint32_t j = y * sz + z;
-    const uint32_t xa = blockIdx.y * k.xchunk;
+    // chunks in descending x order start where the preceding update_E (ascending) finished, on
+    // planes still in L2
+    const uint32_t xa = (k.reverse ? gridDim.y - 1u - blockIdx.y : blockIdx.y) * k.xchunk;
     const uint32_t xb = min(xa + k.xchunk, sx);
     // plus neighbours (common.cl:82-84) in 32-bit wrap arithmetic
     const uint32_t dpy = (y + 1u < sy) ? sz : 0u - (sy - 1u) * sz;

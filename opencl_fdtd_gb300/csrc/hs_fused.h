@@ -33,7 +33,8 @@ struct HSK {
     HSAxis<R> ax[3];
     FastDiv dsz;
     uint32_t rows, xchunk;
-    int32_t write_oS, _pad;
+    int32_t write_oS;
+    int32_t reverse;       // 1: block row b of the grid takes the x chunk gridDim.y - 1 - b
 };
 
 template <typename R>

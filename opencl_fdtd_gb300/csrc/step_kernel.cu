@@ -9,14 +9,14 @@
 //     and every CPML psi), every write goes to the new ones (B), so a block may evaluate cells
 //     another block owns (halo cells) from the same inputs and get the owner's values.
 //   * A block owns the rows [y0, y0 + nown) of all z (a tile) and marches a chunk of x planes.
-//     Its E window is the rows [y0 - 1, y0 + nown], one thread per cell; the H window is
+//     Its E window is the rows [y0 - 1, y0 + nown], one thread per cell (the cells outside the
+//     z faces on the first warps, the z-face cells on the last ones); the H window is
 //     [y0 - 1, y0 + nown), S is formed on the own rows. Row y0 - 1 exists only to give S the
 //     products of its y - 1 neighbours, row y0 + nown only to give H its y + 1 neighbours.
 //   * Iteration x: E_new at plane x (H of plane x and x - 1); H_new and the six Poynting products
 //     at plane x - 1 (E_new of planes x - 1 and x); S at plane x - 1 (products of planes x - 1
-//     and x - 2). The x - 1 values a cell needs from itself stay in registers; E_new of plane
-//     x - 1 and the products go to two small double-buffered shared arrays, so one barrier per
-//     plane orders everything.
+//     and x - 2). The old H of plane x - 1 stays in registers; E_new and the products of a plane
+//     go to two double-buffered shared arrays, so one barrier per plane orders everything.
 //   * Inputs arrive through a ring of shared-memory stages. For each plane the block stages
 //     the rows [y0 - 2, y0 + nown] of H, E, dt/eps (and dt/mu), and of the z-face CPML arrays,
 //     each a contiguous range in the reference's layout (opencl_fdtd/kernels/common.cl:34-52).
@@ -148,11 +148,10 @@ struct StageGeo {
 // Bulk copies of one plane, issued by the 32 lanes of warp 0 (one range per lane), completing
 // on `bar`. A range's tail that is not a whole 16-byte unit of its array is copied with
 // ordinary stores before the arrive that publishes it.
-template <typename R, bool MU>
+template <typename R, int STR, bool MU>
 __device__ __forceinline__ void fill_bulk(const StepK<R> &k, R *st, uint64_t *bar, const StageGeo &g, uint32_t lane)
 {
     constexpr uint64_t V = 16 / sizeof(R);
-    constexpr int STR = StepCfg<R>::STR;
     const R *src = nullptr;
     uint64_t first = 0, count = 0;
     R *dst = nullptr;
@@ -165,13 +164,13 @@ __device__ __forceinline__ void fill_bulk(const StepK<R> &k, R *st, uint64_t *ba
             dst = st + lane * STR;
         }
     } else if (lane < (uint32_t)SG_N) {
-        const int q = (int)lane - SG_NF, type = q >> 2, side = (q >> 1) & 1, uv = q & 1;
+        const int q = (int)lane - SG_NF, side = q >> 2, slot = q & 3;
         const uint32_t T = (uint32_t)(side ? k.ax[2].Tp : k.ax[2].Tn);
         if (T) {
-            src = k.ax[2].psiA[type][side][uv];
+            src = k.ax[2].psiA[slot >> 1][side][slot & 1];
             first = ((uint64_t)g.x * k.sy + g.yH) * T;
             count = (uint64_t)g.rows * T;
-            dst = st + k.zoff[q];
+            dst = st + k.zoff[side] + slot * k.zsz[side];
         }
     }
     uint32_t bytes = 0;
@@ -198,11 +197,10 @@ __device__ __forceinline__ void fill_bulk(const StepK<R> &k, R *st, uint64_t *ba
 
 // The same ranges copied element by element (cp.async) by every thread, rows taken modulo sy;
 // commits one group per call (an empty one when `live` is false).
-template <typename R, bool MU>
+template <typename R, int STR, bool MU>
 __device__ __forceinline__ void fill_async(const StepK<R> &k, R *st, const StageGeo &g, bool live, uint32_t t,
                                            uint32_t nt)
 {
-    constexpr int STR = StepCfg<R>::STR;
     if (live) {
         const uint32_t sz = k.sz, sy = k.sy;
         const uint32_t n = g.rows * sz;
@@ -222,16 +220,13 @@ __device__ __forceinline__ void fill_async(const StepK<R> &k, R *st, const Stage
             const uint32_t T = (uint32_t)(side ? k.ax[2].Tp : k.ax[2].Tn);
             if (!T) continue;
             const uint32_t m = g.rows * T;
+            R *const zb = st + k.zoff[side] + g.zlead[side];
             for (uint32_t q = t; q < m; q += nt) {
                 const uint32_t rq = q / T, ir = q - rq * T;
                 const uint64_t off = ((uint64_t)g.x * sy + (g.yH + rq) % sy) * T + ir;
 #pragma unroll
-                for (int type = 0; type < 2; ++type)
-#pragma unroll
-                    for (int uv = 0; uv < 2; ++uv) {
-                        const int zq = (type * 2 + side) * 2 + uv;
-                        async_elem(st + k.zoff[zq] + g.zlead[side] + q, k.ax[2].psiA[type][side][uv] + off);
-                    }
+                for (int slot = 0; slot < 4; ++slot)
+                    async_elem(zb + slot * k.zsz[side] + q, k.ax[2].psiA[slot >> 1][side][slot & 1] + off);
             }
         }
     }
@@ -251,17 +246,24 @@ __device__ __forceinline__ int step_face(int Tn, int Tp, uint32_t s, uint32_t c,
     return -1;
 }
 
-template <typename R, int DX, bool MU>
-__global__ void __launch_bounds__(StepCfg<R>::MAXT, 1) k_step(const __grid_constant__ StepK<R> k)
+// psi of the x face (u, v) and of the y face (u, v) of one cell and type, zero outside
+template <typename R>
+struct PsiXY {
+    R xu, xv, yu, yv;
+};
+
+template <typename R, typename C, int DX, bool MU>
+__global__ void __launch_bounds__(C::MAXT, C::MINB) k_step(const __grid_constant__ StepK<R> k)
 {
-    constexpr int MAXT = StepCfg<R>::MAXT;
-    constexpr int STR = StepCfg<R>::STR;
+    constexpr int MAXT = C::MAXT;
+    constexpr int STR = C::STR;
     constexpr uint32_t V = 16 / sizeof(R);
     extern __shared__ __align__(128) unsigned char step_smem[];
     R *const stages = reinterpret_cast<R *>(step_smem);
     R *const XE = stages + (size_t)k.nstage * k.stage_elems;     // [2][3][MAXT] E_new of a plane
-    R *const PB = XE + 6 * MAXT;                                 // [2][4][MAXT] products of a plane
-    uint64_t *const full = reinterpret_cast<uint64_t *>(PB + 8 * MAXT);
+    R *const PB = XE + 6 * MAXT;                                 // [2][6][MAXT] products of a plane
+    R *const SC = PB + 12 * MAXT;                                // coefficient tables
+    uint64_t *const full = reinterpret_cast<uint64_t *>(SC + ((k.ncoef + 3u) & ~3u));
 
     const uint32_t sx = k.sx, sy = k.sy, sz = k.sz, syz = k.syz;
     const uint64_t N = k.N;
@@ -276,12 +278,27 @@ __global__ void __launch_bounds__(StepCfg<R>::MAXT, 1) k_step(const __grid_const
     const uint32_t xb = min(xa + k.xchunk, sx);
     const int nit = (int)(xb - xa) + 2;                  // planes xa - 1 .. xb
 
+    // Thread t takes one cell of the E window. The cells outside the z faces come first (row by
+    // row), the z-face cells after them, so that the z-face work falls on as few warps as
+    // possible; q is the cell's position in the window (row r - 1, column z).
     const uint32_t t = threadIdx.x;
-    const bool act = t < (nown + 2u) * sz;
-    const uint32_t rr = act ? t / sz : 0u;
-    const uint32_t z = act ? t - rr * sz : 0u;
+    const uint32_t nrw = nown + 2u;                      // rows of the E window
+    const bool act = t < nrw * sz;
+    uint32_t rr = 0u, z = 0u;
+    if (act) {
+        const uint32_t zi0 = (uint32_t)k.ax[2].Tn, wi = sz - zi0 - (uint32_t)k.ax[2].Tp;
+        if (t < nrw * wi) {
+            rr = t / wi;
+            z = zi0 + (t - rr * wi);
+        } else {
+            const uint32_t f = t - nrw * wi, wf = sz - wi;
+            rr = f / wf;
+            const uint32_t zf = f - rr * wf;
+            z = zf < zi0 ? zf : zf + wi;
+        }
+    }
+    const uint32_t q = rr * sz + z;
     const uint32_t r = rr + 1u;                          // window row (0 is staged only)
-    const uint32_t p = r * sz + z;                       // position in a field slot (before lead)
     const bool hrow = act && r <= nown + 1u;
     const bool own = act && r >= 2u && r <= nown + 1u;
     const uint32_t y = (yH + r) % sy;
@@ -291,8 +308,15 @@ __global__ void __launch_bounds__(StepCfg<R>::MAXT, 1) k_step(const __grid_const
     int fy_side, fz_side;
     const int fy_ir = step_face(k.ax[1].Tn, k.ax[1].Tp, sy, y, fy_side);
     const int fz_ir = step_face(k.ax[2].Tn, k.ax[2].Tp, sz, z, fz_side);
-    const uint32_t fy_T = (uint32_t)(fy_side ? k.ax[1].Tp : k.ax[1].Tn);
-    const uint32_t fz_T = (uint32_t)(fz_side ? k.ax[2].Tp : k.ax[2].Tn);
+    // thickness and coefficient table index (E p0 p1 p2, H p0 p1 p2, T apart) of the cell's y / z
+    // face, the stride of its z slots, and its position in a field slot (before the lead):
+    // recomputed on use
+#define FY_T ((uint32_t)(fy_side ? k.ax[1].Tp : k.ax[1].Tn))
+#define FZ_T ((uint32_t)(fz_side ? k.ax[2].Tp : k.ax[2].Tn))
+#define CY ((uint32_t)(k.coff[1][fy_side] + fy_ir))
+#define CZ ((uint32_t)(k.coff[2][fz_side] + fz_ir))
+#define ZS (k.zsz[fz_side])
+#define P_WIN (q + sz)
     // low bits of the first staged element index of component 0 at plane 0, and of N
     const uint32_t kc0 = yH * sz, nlo = (uint32_t)N;
     auto plane = [&](int q) -> uint32_t {               // plane of iteration q (x taken mod sx)
@@ -314,7 +338,26 @@ __global__ void __launch_bounds__(StepCfg<R>::MAXT, 1) k_step(const __grid_const
         g.zlead[1] = ((g.x * sy + yH) * (uint32_t)k.ax[2].Tp) & (V - 1);
         return g;
     };
+    // psi of the x and y faces of type ty (0: E, 1: H) at plane x, from the A buffers
+    auto psi_xy = [&](int ty, uint32_t x) -> PsiXY<R> {
+        PsiXY<R> v;
+        v.xu = v.xv = v.yu = v.yv = R(0);
+        int xs_;
+        const int xi = step_face(k.ax[0].Tn, k.ax[0].Tp, sx, x, xs_);
+        if (xi >= 0) {
+            const uint64_t ip = (uint64_t)xi * syz + j;
+            v.xu = ldg(k.ax[0].psiA[ty][xs_][0] + ip);
+            v.xv = ldg(k.ax[0].psiA[ty][xs_][1] + ip);
+        }
+        if (fy_ir >= 0) {
+            const uint64_t ip = ((uint64_t)x * FY_T + (uint32_t)fy_ir) * sz + z;
+            v.yu = ldg(k.ax[1].psiA[ty][fy_side][0] + ip);
+            v.yv = ldg(k.ax[1].psiA[ty][fy_side][1] + ip);
+        }
+        return v;
+    };
 
+    for (uint32_t q = t; q < k.ncoef; q += nt) SC[q] = k.coef[q];
     if (t == 0) {
         for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
         mbar_fence_init();
@@ -329,58 +372,52 @@ __global__ void __launch_bounds__(StepCfg<R>::MAXT, 1) k_step(const __grid_const
         hy_m = ldg(k.HA + N + i);
         hz_m = ldg(k.HA + 2 * N + i);
     }
-    // psi_E of the x and y faces for the next E evaluation, psi_H (x, y, z faces) for the next
+    // psi_E of the x and y faces for the next E evaluation; psi_H (x, y, z faces) for the next
     // H evaluation
-    R pe[4] = {R(0), R(0), R(0), R(0)};
-    R ph[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};
-    auto load_pe = [&](uint32_t x) {
-        int xs_;
-        const int xi = step_face(k.ax[0].Tn, k.ax[0].Tp, sx, x, xs_);
-        pe[0] = pe[1] = pe[2] = pe[3] = R(0);
-        if (xi >= 0) {
-            const uint64_t ip = (uint64_t)xi * syz + j;
-            pe[0] = ldg(k.ax[0].psiA[0][xs_][0] + ip);
-            pe[1] = ldg(k.ax[0].psiA[0][xs_][1] + ip);
-        }
-        if (fy_ir >= 0) {
-            const uint64_t ip = ((uint64_t)x * fy_T + fy_ir) * sz + z;
-            pe[2] = ldg(k.ax[1].psiA[0][fy_side][0] + ip);
-            pe[3] = ldg(k.ax[1].psiA[0][fy_side][1] + ip);
-        }
-    };
-    if (act) load_pe(plane(0));
+    PsiXY<R> pe = {R(0), R(0), R(0), R(0)}, ph = {R(0), R(0), R(0), R(0)};
+    R phzu = R(0), phzv = R(0);
+    if (act) pe = psi_xy(0, plane(0));
 
     // first stages
     const int npre = NS < nit ? NS : nit;
     if (tma) {
         if (t < 32)
-            for (int q = 0; q < npre; ++q) fill_bulk<R, MU>(k, stages + (size_t)q * k.stage_elems, &full[q], geo(q), t);
+            for (int q = 0; q < npre; ++q)
+                fill_bulk<R, STR, MU>(k, stages + (size_t)q * k.stage_elems, &full[q], geo(q), t);
     } else {
-        for (int q = 0; q < NS; ++q) fill_async<R, MU>(k, stages + (size_t)q * k.stage_elems, geo(q), q < nit, t, nt);
+        for (int q = 0; q < NS; ++q)
+            fill_async<R, STR, MU>(k, stages + (size_t)q * k.stage_elems, geo(q), q < nit, t, nt);
         async_wait_n(NS - 1);
         __syncthreads();
     }
 
-    R ex_m = R(0), ey_m = R(0), ez_m = R(0);            // E_new of plane x - 1 at the cell
     R cx_m = R(0), cy_m = R(0), cz_m = R(0);            // dt/mu of plane x - 1
-    R p_yx = R(0), p_zx = R(0);                          // products yx, zx of plane x - 2
+    // the cell's 32-bit index at the planes x and x - 1 (the written arrays are addressed from
+    // their per-component bases, which the kernel parameters give block-uniformly)
+    uint32_t x = plane(0);
     int it = 0;
+    uint32_t sp = 0;                                     // stage slot (bits 1..) and its parity (bit 0)
     bool abort = false;
     for (; it < nit; ++it) {
-        const uint32_t x = plane(it);
-        const int slot = it % NS;
+        const uint32_t slot = sp >> 1;
         R *const st = stages + (size_t)slot * k.stage_elems;
         bool failed = false;
-        if (tma) failed = !stage_wait(&full[slot], (uint32_t)(it / NS) & 1u, k.wait_ns, k.status);
+        if (tma) failed = !stage_wait(&full[slot], sp & 1u, k.wait_ns, k.status);
         const uint32_t xs = x * syz;
-        const R *const b0 = st + ((kc0 + xs) & (V - 1)) + p;
-        const R *const b1 = st + ((kc0 + xs + nlo) & (V - 1)) + p;
-        const R *const b2 = st + ((kc0 + xs + 2u * nlo) & (V - 1)) + p;
+        const uint32_t xm = x ? x - 1u : sx - 1u;
+        const uint32_t ic = xs + j, im = xm * syz + j;  // the cell at planes x and x - 1
+        const uint32_t xo = (uint32_t)(it & 1) * (uint32_t)MAXT;   // this plane's XE / PB halves
+        const R *const b0 = st + ((kc0 + xs) & (V - 1)) + P_WIN;
+        const R *const b1 = st + ((kc0 + xs + nlo) & (V - 1)) + P_WIN;
+        const R *const b2 = st + ((kc0 + xs + 2u * nlo) & (V - 1)) + P_WIN;
         const bool ein = it >= 1 && it <= nit - 2;       // plane x is in the block's chunk
         const bool hin = it >= 2;                        // plane x - 1 is in the block's chunk
         int xf_side;
         const int xf_ir = step_face(k.ax[0].Tn, k.ax[0].Tp, sx, x, xf_side);
-        const uint32_t zrow = ((x * sy + yH) * fz_T) & (V - 1);   // lead of this cell's z slots
+        R *const xe_c = XE + xo * 3u + q;                // E_new of plane x
+        const R *const xe_p = XE + (xo ^ (uint32_t)MAXT) * 3u + q;   // of plane x - 1
+        R *const pb_c = PB + xo * 6u + q;                // products of plane x - 1
+        const R *const pb_p = PB + (xo ^ (uint32_t)MAXT) * 6u + q;   // of plane x - 2
 
         // ---- E_new at plane x (update_e.cl:39-107) ----
         R hx = R(0), hy = R(0), hz = R(0), ex = R(0), ey = R(0), ez = R(0);
@@ -405,36 +442,36 @@ __global__ void __launch_bounds__(StepCfg<R>::MAXT, 1) k_step(const __grid_const
             R px = R(0), py = R(0), pz = R(0);
             const bool wr = own && ein;
             if (xf_ir >= 0) {
-                const R *const *tb = k.ax[0].tab[0][xf_side];
+                const uint32_t T = (uint32_t)(xf_side ? k.ax[0].Tp : k.ax[0].Tn);
+                const uint32_t c = (uint32_t)(k.coff[0][xf_side] + xf_ir);
                 R su, sv;
-                face_update<R, true, 0>(ldg(tb[0] + xf_ir), ldg(tb[1] + xf_ir), ldg(tb[2] + xf_ir), pe[0], pe[1],
+                face_update<R, true, 0>(SC[c], SC[c + T], SC[c + 2 * T], pe.xu, pe.xv,
                                         su, sv, d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
                 if (wr) {
-                    const uint64_t ip = (uint64_t)xf_ir * syz + j;
+                    const uint32_t ip = (uint32_t)xf_ir * syz + j;
                     k.ax[0].psiB[0][xf_side][0][ip] = su;
                     k.ax[0].psiB[0][xf_side][1][ip] = sv;
                 }
             }
             if (fy_ir >= 0) {
-                const R *const *tb = k.ax[1].tab[0][fy_side];
+                const uint32_t c = CY, T = FY_T;
                 R su, sv;
-                face_update<R, true, 1>(ldg(tb[0] + fy_ir), ldg(tb[1] + fy_ir), ldg(tb[2] + fy_ir), pe[2], pe[3],
+                face_update<R, true, 1>(SC[c], SC[c + T], SC[c + 2 * T], pe.yu, pe.yv,
                                         su, sv, d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
                 if (wr) {
-                    const uint64_t ip = ((uint64_t)x * fy_T + fy_ir) * sz + z;
+                    const uint32_t ip = (x * T + (uint32_t)fy_ir) * sz + z;
                     k.ax[1].psiB[0][fy_side][0][ip] = su;
                     k.ax[1].psiB[0][fy_side][1][ip] = sv;
                 }
             }
             if (fz_ir >= 0) {
-                const R *const *tb = k.ax[2].tab[0][fz_side];
-                const uint32_t zq = zrow + r * fz_T + (uint32_t)fz_ir;
-                const R ou = st[k.zoff[fz_side * 2 + 0] + zq], ov = st[k.zoff[fz_side * 2 + 1] + zq];
+                const uint32_t c = CZ, T = FZ_T;
+                const R *const zb = st + k.zoff[fz_side] + r * T + (uint32_t)fz_ir + (((x * sy + yH) * T) & (V - 1));
                 R su, sv;
-                face_update<R, true, 2>(ldg(tb[0] + fz_ir), ldg(tb[1] + fz_ir), ldg(tb[2] + fz_ir), ou, ov,
+                face_update<R, true, 2>(SC[c], SC[c + T], SC[c + 2 * T], zb[0], zb[ZS],
                                         su, sv, d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
                 if (wr) {
-                    const uint64_t ip = ((uint64_t)x * sy + y) * fz_T + fz_ir;
+                    const uint32_t ip = (x * sy + y) * T + (uint32_t)fz_ir;
                     k.ax[2].psiB[0][fz_side][0][ip] = su;
                     k.ax[2].psiB[0][fz_side][1][ip] = sv;
                 }
@@ -455,25 +492,23 @@ __global__ void __launch_bounds__(StepCfg<R>::MAXT, 1) k_step(const __grid_const
                 }
             }
             if (wr) {
-                R *const e = k.EB + ((uint64_t)xs + j);
-                e[0] = ex;
-                e[N] = ey;
-                e[2 * N] = ez;
+                k.EB[ic] = ex;
+                (k.EB + N)[ic] = ey;
+                (k.EB + 2 * N)[ic] = ez;
             }
-            R *const xe = XE + (it & 1) * 3 * MAXT + t;
-            xe[0] = ex;
-            xe[MAXT] = ey;
-            xe[2 * MAXT] = ez;
+            xe_c[0] = ex;
+            xe_c[MAXT] = ey;
+            xe_c[2 * MAXT] = ez;
         }
-        if (act && it + 1 < nit) load_pe(plane(it + 1));
+        const uint32_t xn = x + 1u == sx ? 0u : x + 1u;
+        if (act && it + 1 < nit) pe = psi_xy(0, xn);
 
-        // ---- H_new and the products at plane xm = x - 1 (update_h.cl:36-155) ----
-        R os0 = R(0), os1 = R(0), os2 = R(0), os3 = R(0), os4 = R(0), os5 = R(0);
+        // ---- H_new and the products at plane x - 1 (update_h.cl:36-155) ----
         if (hrow && it >= 1 && !failed) {
-            const uint32_t xm = x ? x - 1u : sx - 1u;
-            const R *const xe = XE + ((it - 1) & 1) * 3 * MAXT;
-            const R rxy = xe[t + sz], rzy = xe[2 * MAXT + t + sz];
-            const R rxz = xe[(int)t + dpz], ryz = xe[MAXT + (int)t + dpz];
+            // E_new of plane x - 1: the cell and its y + 1, z + 1 neighbours
+            const R ex_m = xe_p[0], ey_m = xe_p[MAXT], ez_m = xe_p[2 * MAXT];
+            const R rxy = xe_p[sz], rzy = xe_p[2 * MAXT + sz];
+            const R rxz = xe_p[dpz], ryz = xe_p[MAXT + dpz];
             R d_xy = rxy - ex_m;
             R d_xz = rxz - ex_m;
             R d_yx = ey - ey_m;
@@ -482,7 +517,11 @@ __global__ void __launch_bounds__(StepCfg<R>::MAXT, 1) k_step(const __grid_const
             R d_zy = rzy - ez_m;
             if (DX != 0) {
                 R ix = k.inv_d, iy = k.inv_d, iz = k.inv_d;
-                if (DX == 2) { ix = ldg(k.inv_de[0] + xm); iy = ldg(k.inv_de[1] + y); iz = ldg(k.inv_de[2] + z); }
+                if (DX == 2) {
+                    ix = ldg(k.inv_de[0] + xm);
+                    iy = ldg(k.inv_de[1] + y);
+                    iz = ldg(k.inv_de[2] + z);
+                }
                 d_xy = d_xy * iy; d_xz = d_xz * iz; d_yx = d_yx * ix;
                 d_yz = d_yz * iz; d_zx = d_zx * ix; d_zy = d_zy * iy;
             }
@@ -491,34 +530,35 @@ __global__ void __launch_bounds__(StepCfg<R>::MAXT, 1) k_step(const __grid_const
             int mf_side;
             const int mf_ir = step_face(k.ax[0].Tn, k.ax[0].Tp, sx, xm, mf_side);
             if (mf_ir >= 0) {
-                const R *const *tb = k.ax[0].tab[1][mf_side];
+                const uint32_t T = (uint32_t)(mf_side ? k.ax[0].Tp : k.ax[0].Tn);
+                const uint32_t c = (uint32_t)(k.coff[0][mf_side] + mf_ir) + 3u * T;
                 R su, sv;
-                face_update<R, false, 0>(ldg(tb[0] + mf_ir), ldg(tb[1] + mf_ir), ldg(tb[2] + mf_ir), ph[0], ph[1],
+                face_update<R, false, 0>(SC[c], SC[c + T], SC[c + 2 * T], ph.xu, ph.xv,
                                          su, sv, d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
                 if (wr) {
-                    const uint64_t ip = (uint64_t)mf_ir * syz + j;
+                    const uint32_t ip = (uint32_t)mf_ir * syz + j;
                     k.ax[0].psiB[1][mf_side][0][ip] = su;
                     k.ax[0].psiB[1][mf_side][1][ip] = sv;
                 }
             }
             if (fy_ir >= 0) {
-                const R *const *tb = k.ax[1].tab[1][fy_side];
+                const uint32_t T = FY_T, c = CY + 3u * T;
                 R su, sv;
-                face_update<R, false, 1>(ldg(tb[0] + fy_ir), ldg(tb[1] + fy_ir), ldg(tb[2] + fy_ir), ph[2], ph[3],
+                face_update<R, false, 1>(SC[c], SC[c + T], SC[c + 2 * T], ph.yu, ph.yv,
                                          su, sv, d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
                 if (wr) {
-                    const uint64_t ip = ((uint64_t)xm * fy_T + fy_ir) * sz + z;
+                    const uint32_t ip = (xm * T + (uint32_t)fy_ir) * sz + z;
                     k.ax[1].psiB[1][fy_side][0][ip] = su;
                     k.ax[1].psiB[1][fy_side][1][ip] = sv;
                 }
             }
             if (fz_ir >= 0) {
-                const R *const *tb = k.ax[2].tab[1][fz_side];
+                const uint32_t T = FZ_T, c = CZ + 3u * T;
                 R su, sv;
-                face_update<R, false, 2>(ldg(tb[0] + fz_ir), ldg(tb[1] + fz_ir), ldg(tb[2] + fz_ir), ph[4], ph[5],
+                face_update<R, false, 2>(SC[c], SC[c + T], SC[c + 2 * T], phzu, phzv,
                                          su, sv, d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
                 if (wr) {
-                    const uint64_t ip = ((uint64_t)xm * sy + y) * fz_T + fz_ir;
+                    const uint32_t ip = (xm * sy + y) * T + (uint32_t)fz_ir;
                     k.ax[2].psiB[1][fz_side][0][ip] = su;
                     k.ax[2].psiB[1][fz_side][1][ip] = sv;
                 }
@@ -533,54 +573,44 @@ __global__ void __launch_bounds__(StepCfg<R>::MAXT, 1) k_step(const __grid_const
                 hyn = hy_m - k.dt * ((d_xz - d_zx) - py);
                 hzn = hz_m - k.dt * ((d_yx - d_xy) - pz);
             }
-            const uint64_t i = (uint64_t)xm * syz + j;
             if (wr) {
-                R *const h = k.HB + i;
-                h[0] = hxn;
-                h[N] = hyn;
-                h[2 * N] = hzn;
+                k.HB[im] = hxn;
+                (k.HB + N)[im] = hyn;
+                (k.HB + 2 * N)[im] = hzn;
             }
             if (k.poynt) {
                 const R ahx = hxn + hx_m, ahy = hyn + hy_m, ahz = hzn + hz_m;
-                os0 = (ey + ey_m) * ahz;
-                os3 = (-(ez + ez_m)) * ahy;
-                os1 = (rzy + ez_m) * ahx;
-                os4 = (-(rxy + ex_m)) * ahz;
-                os2 = (rxz + ex_m) * ahy;
-                os5 = (-(ryz + ey_m)) * ahx;
+                const R os0 = (ey + ey_m) * ahz;
+                const R os3 = (-(ez + ez_m)) * ahy;
+                const R os1 = (rzy + ez_m) * ahx;
+                const R os4 = (-(rxy + ex_m)) * ahz;
+                const R os2 = (rxz + ex_m) * ahy;
+                const R os5 = (-(ryz + ey_m)) * ahx;
                 if (wr && k.write_oS) {
-                    R *const o = k.oS + i;
-                    o[0] = os0;
-                    o[N] = os1;
-                    o[2 * N] = os2;
-                    o[3 * N] = os3;
-                    o[4 * N] = os4;
-                    o[5 * N] = os5;
+                    k.oS[im] = os0;
+                    (k.oS + N)[im] = os1;
+                    (k.oS + 2 * N)[im] = os2;
+                    (k.oS + 3 * N)[im] = os3;
+                    (k.oS + 4 * N)[im] = os4;
+                    (k.oS + 5 * N)[im] = os5;
                 }
-                R *const pb = PB + (it & 1) * 4 * MAXT + t;
-                pb[0] = os0;
-                pb[MAXT] = os3;
-                pb[2 * MAXT] = os1;
-                pb[3 * MAXT] = os5;
+                // the products in the reference's order xy, yz, zx, xz, yx, zy (update_h.cl:142-147)
+                pb_c[0] = os0;
+                pb_c[MAXT] = os1;
+                pb_c[2 * MAXT] = os2;
+                pb_c[3 * MAXT] = os3;
+                pb_c[4 * MAXT] = os4;
+                pb_c[5 * MAXT] = os5;
             }
         }
         // what the next H evaluation (plane x) needs from this plane
         if (act && !failed) {
-            ph[0] = ph[1] = ph[2] = ph[3] = R(0);
-            if (xf_ir >= 0) {
-                const uint64_t ip = (uint64_t)xf_ir * syz + j;
-                ph[0] = ldg(k.ax[0].psiA[1][xf_side][0] + ip);
-                ph[1] = ldg(k.ax[0].psiA[1][xf_side][1] + ip);
-            }
-            if (fy_ir >= 0) {
-                const uint64_t ip = ((uint64_t)x * fy_T + fy_ir) * sz + z;
-                ph[2] = ldg(k.ax[1].psiA[1][fy_side][0] + ip);
-                ph[3] = ldg(k.ax[1].psiA[1][fy_side][1] + ip);
-            }
+            ph = psi_xy(1, x);
             if (fz_ir >= 0) {
-                const uint32_t zq = zrow + r * fz_T + (uint32_t)fz_ir;
-                ph[4] = st[k.zoff[(2 + fz_side) * 2 + 0] + zq];
-                ph[5] = st[k.zoff[(2 + fz_side) * 2 + 1] + zq];
+                const uint32_t T = FZ_T;
+                const R *const zb = st + k.zoff[fz_side] + r * T + (uint32_t)fz_ir + (((x * sy + yH) * T) & (V - 1));
+                phzu = zb[2 * ZS];
+                phzv = zb[3 * ZS];
             }
             if (MU) {
                 cx_m = b0[SG_M * STR];
@@ -596,28 +626,27 @@ __global__ void __launch_bounds__(StepCfg<R>::MAXT, 1) k_step(const __grid_const
         if (abort) break;
         // this stage is free: stage the plane of iteration it + NS into it
         if (tma) {
-            if (t < 32 && it + NS < nit) fill_bulk<R, MU>(k, st, &full[slot], geo(it + NS), t);
+            if (t < 32 && it + NS < nit) fill_bulk<R, STR, MU>(k, st, &full[slot], geo(it + NS), t);
         } else {
-            fill_async<R, MU>(k, st, geo(it + NS), it + NS < nit, t, nt);
+            fill_async<R, STR, MU>(k, st, geo(it + NS), it + NS < nit, t, nt);
         }
 
-        // ---- S at plane x - 1 (update_s.cl:33-36) ----
+        // ---- S at plane x - 1 (update_s.cl:33-36): products of planes x - 1 (this iteration's
+        // buffer) and x - 2 (the previous one) ----
         if (k.poynt && own && hin) {
-            const R *const pb = PB + (it & 1) * 4 * MAXT;
-            const R xy_y = pb[t - sz], zy_y = pb[3 * MAXT + t - sz];
-            const R xz_z = pb[MAXT + (int)t + dmz], yz_z = pb[2 * MAXT + (int)t + dmz];
-            const uint32_t xm = x ? x - 1u : sx - 1u;
-            R *const s = k.S + ((uint64_t)xm * syz + j);
-            s[0] = (((os0 + os3) + xy_y) + xz_z) * k.sf;
-            s[N] = (((os1 + os4) + yz_z) + p_yx) * k.sf;
-            s[2 * N] = (((os2 + os5) + p_zx) + zy_y) * k.sf;
+            k.S[im] = (((pb_c[0] + pb_c[3 * MAXT]) + pb_c[-(int)sz]) + pb_c[3 * MAXT + dmz]) * k.sf;
+            (k.S + N)[im] = (((pb_c[MAXT] + pb_c[4 * MAXT]) + pb_c[MAXT + dmz]) + pb_p[4 * MAXT]) * k.sf;
+            (k.S + 2 * N)[im] = (((pb_c[2 * MAXT] + pb_c[5 * MAXT]) + pb_p[2 * MAXT]) + pb_c[5 * MAXT - (int)sz]) * k.sf;
         }
-        p_yx = os4;
-        p_zx = os2;
-        ex_m = ex;
-        ey_m = ey;
-        ez_m = ez;
+        x = xn;
+        sp = (slot + 1u == (uint32_t)NS) ? ((sp & 1u) ^ 1u) : sp + 2u;
     }
+#undef FY_T
+#undef FZ_T
+#undef CY
+#undef CZ
+#undef ZS
+#undef P_WIN
     if (abort) {
         // wait (bounded) for the copies still in flight before the block's memory is released
         if (tma) {
@@ -638,20 +667,28 @@ __global__ void __launch_bounds__(StepCfg<R>::MAXT, 1) k_step(const __grid_const
 }
 
 // ---- host side -------------------------------------------------------------------------------
-template <typename R>
-uint32_t step_max_rows(uint32_t sz)
+template <typename C>
+static uint32_t max_rows_of(uint32_t sz, uint32_t V)
 {
-    constexpr uint32_t V = 16 / sizeof(R);
-    const uint32_t cap = (uint32_t)StepCfg<R>::STR - 2u * (V - 1u);   // staged elements per slot
-    if (!sz || 4u * sz > cap || 3u * sz > (uint32_t)StepCfg<R>::MAXT) return 0;
-    const uint32_t by_slot = cap / sz - 3u, by_threads = (uint32_t)StepCfg<R>::MAXT / sz - 2u;
+    const uint32_t cap = (uint32_t)C::STR - 2u * (V - 1u);   // staged elements per slot
+    if (!sz || 4u * sz > cap || 3u * sz > (uint32_t)C::MAXT) return 0;
+    const uint32_t by_slot = cap / sz - 3u, by_threads = (uint32_t)C::MAXT / sz - 2u;
     return by_slot < by_threads ? by_slot : by_threads;
 }
 
 template <typename R>
-size_t step_smem_bytes(uint32_t nstage, uint32_t stage_elems)
+uint32_t step_max_rows(int shape, uint32_t sz)
 {
-    return ((size_t)nstage * stage_elems + 14u * (size_t)StepCfg<R>::MAXT) * sizeof(R) +
+    constexpr uint32_t V = 16 / sizeof(R);
+    if (sizeof(R) == 8) return max_rows_of<StepF64>(sz, V);
+    return shape == STEP_SHAPE_SMALL ? max_rows_of<StepSmall>(sz, V) : max_rows_of<StepBig>(sz, V);
+}
+
+template <typename R>
+size_t step_smem_bytes(int shape, uint32_t nstage, uint32_t stage_elems, uint32_t ncoef)
+{
+    const size_t maxt = sizeof(R) == 8 ? StepF64::MAXT : shape == STEP_SHAPE_SMALL ? StepSmall::MAXT : StepBig::MAXT;
+    return ((size_t)nstage * stage_elems + 18u * maxt + ((ncoef + 3u) & ~3u)) * sizeof(R) +
            (size_t)STEP_MAX_STAGES * sizeof(uint64_t);
 }
 
@@ -661,7 +698,7 @@ uint32_t step_threads(uint32_t rows, uint32_t sz)
     return (n + 31u) / 32u * 32u;
 }
 
-template <typename R, int DX, bool MU>
+template <typename R, typename C, int DX, bool MU>
 static cudaError_t launch_one(const StepK<R> &k, uint32_t threads, size_t smem, cudaStream_t st)
 {
     static int configured[64];
@@ -670,33 +707,47 @@ static cudaError_t launch_one(const StepK<R> &k, uint32_t threads, size_t smem, 
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     if (configured[dev] < (int)smem) {
-        e = cudaFuncSetAttribute(k_step<R, DX, MU>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(k_step<R, C, DX, MU>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured[dev] = (int)smem;
     }
     const dim3 g(k.ntile, (k.sx + k.xchunk - 1) / k.xchunk, 1);
-    k_step<R, DX, MU><<<g, threads, smem, st>>>(k);
+    k_step<R, C, DX, MU><<<g, threads, smem, st>>>(k);
     return cudaGetLastError();
 }
 
-template <typename R>
-cudaError_t launch_step(const StepK<R> &k, int dxmode, bool mu, uint32_t threads, size_t smem, cudaStream_t st)
+template <typename R, typename C>
+static cudaError_t launch_shape(const StepK<R> &k, int dxmode, bool mu, uint32_t threads, size_t smem,
+                                cudaStream_t st)
 {
     if (mu) {
-        if (dxmode == 0) return launch_one<R, 0, true>(k, threads, smem, st);
-        if (dxmode == 1) return launch_one<R, 1, true>(k, threads, smem, st);
-        return launch_one<R, 2, true>(k, threads, smem, st);
+        if (dxmode == 0) return launch_one<R, C, 0, true>(k, threads, smem, st);
+        if (dxmode == 1) return launch_one<R, C, 1, true>(k, threads, smem, st);
+        return launch_one<R, C, 2, true>(k, threads, smem, st);
     }
-    if (dxmode == 0) return launch_one<R, 0, false>(k, threads, smem, st);
-    if (dxmode == 1) return launch_one<R, 1, false>(k, threads, smem, st);
-    return launch_one<R, 2, false>(k, threads, smem, st);
+    if (dxmode == 0) return launch_one<R, C, 0, false>(k, threads, smem, st);
+    if (dxmode == 1) return launch_one<R, C, 1, false>(k, threads, smem, st);
+    return launch_one<R, C, 2, false>(k, threads, smem, st);
 }
 
-template uint32_t step_max_rows<float>(uint32_t);
-template uint32_t step_max_rows<double>(uint32_t);
-template size_t step_smem_bytes<float>(uint32_t, uint32_t);
-template size_t step_smem_bytes<double>(uint32_t, uint32_t);
-template cudaError_t launch_step<float>(const StepK<float> &, int, bool, uint32_t, size_t, cudaStream_t);
-template cudaError_t launch_step<double>(const StepK<double> &, int, bool, uint32_t, size_t, cudaStream_t);
+template <>
+cudaError_t launch_step<float>(const StepK<float> &k, int shape, int dxmode, bool mu, uint32_t threads,
+                               size_t smem, cudaStream_t st)
+{
+    if (shape == STEP_SHAPE_SMALL) return launch_shape<float, StepSmall>(k, dxmode, mu, threads, smem, st);
+    return launch_shape<float, StepBig>(k, dxmode, mu, threads, smem, st);
+}
+
+template <>
+cudaError_t launch_step<double>(const StepK<double> &k, int, int dxmode, bool mu, uint32_t threads, size_t smem,
+                                cudaStream_t st)
+{
+    return launch_shape<double, StepF64>(k, dxmode, mu, threads, smem, st);
+}
+
+template uint32_t step_max_rows<float>(int, uint32_t);
+template uint32_t step_max_rows<double>(int, uint32_t);
+template size_t step_smem_bytes<float>(int, uint32_t, uint32_t, uint32_t);
+template size_t step_smem_bytes<double>(int, uint32_t, uint32_t, uint32_t);
 
 }  // namespace fdtd

@@ -618,26 +618,32 @@ class Simulation:
 
     def tune(self, xchunk: int = None, slab: int = None, fused_rows: int = None,
              fused_xchunk: int = None, hs_xchunk: int = None, hs_prefetch: bool = None,
-             fused_stages: int = None, fused_tma: bool = None):
+             fused_stages: int = None, fused_tma: bool = None, fused_shape: int = None,
+             hs_reverse: bool = None):
         """Kernel tiling (None keeps a value); results do not depend on it.
 
         fused_rows / fused_xchunk / fused_stages: own y rows of a one-pass step tile, x planes
         of a block, planes in its shared-memory ring (0: automatic); fused_tma: stage the rows
-        of non-wrapping tiles with bulk asynchronous copies (default) or per element."""
+        of non-wrapping tiles with bulk asynchronous copies (default) or per element;
+        fused_shape: block shape (1 large, 2 small, 0 automatic); hs_reverse: the H+S kernel of
+        the 'hs' path takes its x chunks in descending order (default) or ascending."""
         for key, val in ((_lib.FDTD_TUNE_XCHUNK, xchunk), (_lib.FDTD_TUNE_SLAB, slab),
                          (_lib.FDTD_TUNE_FUSED_ROWS, fused_rows),
                          (_lib.FDTD_TUNE_FUSED_XCHUNK, fused_xchunk),
                          (_lib.FDTD_TUNE_HS_XCHUNK, hs_xchunk),
                          (_lib.FDTD_TUNE_HS_PREFETCH, None if hs_prefetch is None else int(hs_prefetch)),
                          (_lib.FDTD_TUNE_FUSED_STAGES, fused_stages),
-                         (_lib.FDTD_TUNE_FUSED_TMA, None if fused_tma is None else int(fused_tma))):
+                         (_lib.FDTD_TUNE_FUSED_TMA, None if fused_tma is None else int(fused_tma)),
+                         (_lib.FDTD_TUNE_FUSED_SHAPE, fused_shape),
+                         (_lib.FDTD_TUNE_HS_REVERSE, None if hs_reverse is None else int(hs_reverse))):
             if val is not None:
                 _lib.check(self._lib.fdtd_plan_tune(self._plan, key, int(val)))
 
     def tuning(self, key: str) -> int:
         """Current value of a tuning key ('fused_rows', 'hs_xchunk', ...) or of a read-only key:
         'last_run_path' (0 none, 1 per-update, 2 H+S, 3 one-pass) and 'step_rows',
-        'step_xchunk', 'step_stages', 'step_threads' (tiling of the last one-pass launch)."""
+        'step_xchunk', 'step_stages', 'step_threads', 'step_shape' (tiling of the last one-pass
+        launch)."""
         name = key.upper()
         const = getattr(_lib, "FDTD_GET_" + name, None)
         if const is None:

@@ -45,13 +45,14 @@ def _same_state(a, b, poynting):
             assert torch.equal(u1, u2) and torch.equal(v1, v2), fld
 
 
-# (rows per tile, x chunk, stages, bulk copies)
-TILINGS = [(0, 0, 0, 1), (1, 3, 2, 1), (2, 1, 3, 0), (3, 2, 0, 1), (5, 7, 2, 0), (4, 5, 4, 1)]
+# (rows per tile, x chunk, stages, bulk copies, block shape)
+TILINGS = [(0, 0, 0, 1, 0), (1, 3, 2, 1, 2), (2, 1, 3, 0, 1), (3, 2, 0, 1, 2), (5, 7, 2, 0, 1), (4, 5, 4, 1, 1),
+           (0, 0, 0, 1, 1), (0, 4, 3, 1, 2)]
 
 
 def _tune(sim, tiling):
-    rows, xc, ns, tma = tiling
-    sim.tune(fused_rows=rows, fused_xchunk=xc, fused_stages=ns, fused_tma=bool(tma))
+    rows, xc, ns, tma, shape = tiling
+    sim.tune(fused_rows=rows, fused_xchunk=xc, fused_stages=ns, fused_tma=bool(tma), fused_shape=shape)
 
 
 @pytest.mark.parametrize("name", ["c1_small", "pml_mixed", "periodic_pec_poynting", "nonuniform",
@@ -73,7 +74,8 @@ def test_fused_equals_per_call_loop(name, tiling, nsteps):
 
 @pytest.mark.parametrize("shape,faces,T", [((9, 40, 37), "xyz", (3, 5, 6)), ((6, 23, 18), "yz", (2, 4, 7)),
                                            ((7, 31, 20), "z", (0, 0, 9)), ((5, 17, 11), "", (0, 0, 0))])
-@pytest.mark.parametrize("tiling", [(1, 2, 2, 1), (3, 4, 3, 1), (6, 0, 0, 1), (2, 3, 4, 0)])
+@pytest.mark.parametrize("tiling", [(1, 2, 2, 1, 2), (3, 4, 3, 1, 1), (6, 0, 0, 1, 0), (2, 3, 4, 0, 2),
+                                    (0, 0, 0, 1, 2)])
 @pytest.mark.parametrize("dtype,mu", [(numpy.float32, False), (numpy.float32, True), (numpy.float64, True)])
 def test_fused_many_tiles(shape, faces, T, tiling, dtype, mu):
     """Grids with many tiles, most of them staged by bulk copies, CPML faces of uneven
