@@ -67,6 +67,13 @@ def parse():
     ap.add_argument("--c4-chunk", type=int, default=100, help="c4: steps per captured launch")
     ap.add_argument("--c5-runs", type=int, default=200, help="c5: teacher runs at 128^3")
     ap.add_argument("--c5-steps", type=int, default=2000, help="c5: timed steps of the c2 cavity forms")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the parity, batched and learned-boundary sections of the default run")
+    ap.add_argument("--parity-steps", type=int, default=400, help="steps of the float64 comparison run")
+    ap.add_argument("--extras-variants", type=int, default=16, help="batched section: c4 variants")
+    ap.add_argument("--extras-steps", type=int, default=400, help="batched section: steps per variant")
+    ap.add_argument("--learned-runs", type=int, default=40, help="learned section: teacher runs")
+    ap.add_argument("--learned-steps", type=int, default=1000, help="learned section: timed steps")
     ap.add_argument("--path", choices=["fused", "slab", "hs", "dropin", "default", "all"], default="default",
                     help="default = per-call loop (per-kernel timing) + Simulation.run (hs path); "
                          "slab = run over the per-update kernels; fused = the opt-in fused step")
@@ -161,6 +168,35 @@ def algorithmic_bytes(N: int, face_cells: int, elem: int, poynting: bool):
     return {"k_bulk_e": e, "k_bulk_h": h, "k_bulk_s": s, "k_bulk_hs": hs}, step
 
 
+# FP64 DFT monitor of the c2 ringdown (the north star's "FP64 DFT monitor at 5 interior points"):
+# E_y at the cavity centre and at four points two lattice constants away in x and y, transformed at
+# the source's centre frequency and 5% either side of it
+MONITOR_OFFSETS = ((0, 0), (20, 0), (-20, 0), (0, 20), (0, -20))
+MONITOR_DESC = "FP64 DFT of E_y at 5 interior points (centre, +-20 cells in x and y), 3 frequencies, every step"
+
+
+def monitor_points(wl):
+    shape = wl["shape"]
+    N = int(numpy.prod(shape))
+    c = numpy.unravel_index(wl["source_index"] % N, shape)
+    return [(1, (int(c[0]) + dx, int(c[1]) + dy, int(c[2]))) for dx, dy in MONITOR_OFFSETS]
+
+
+def monitor_omegas():
+    w0 = 2 * math.pi * 40.0 / 1550.0
+    return [0.95 * w0, w0, 1.05 * w0]
+
+
+def workload_config(wl, fc: int, elem: int, poynting: bool):
+    """The workload as both arms report it (the same keys and values)."""
+    N = int(numpy.prod(wl["shape"]))
+    cfg = {"workload": wl["describe"], "grid": list(wl["shape"]), "cells": N, "cpml_face_cells": fc,
+           "l2": "inputs (~%.0f MB of fields) larger than the 129 MB L2; no flush" % (3 * N * elem * (6 if poynting else 3) / 1e6)}
+    if wl["name"] == "c2":
+        cfg["monitor"] = MONITOR_DESC
+    return cfg
+
+
 def cpu_sample(wl, seconds: float, nthreads: int):
     """Time full-grid steps of the reference's CPU kernels (replay) or the C restatement."""
     from oracle import ref_replay
@@ -176,10 +212,18 @@ def cpu_sample(wl, seconds: float, nthreads: int):
         kind = "port"
     N = int(numpy.prod(wl["shape"]))
     ind = wl["source_index"]
+    mon_idx = numpy.array([c * N + int(numpy.ravel_multi_index(p, wl["shape"])) for c, p in monitor_points(wl)]) \
+        if wl["name"] == "c2" else None
+    om = numpy.array(monitor_omegas())
+    acc = numpy.zeros((5, 3), numpy.complex128)
+    dt = float(getattr(sim, "dt", 0.0) or 0.0)
 
     def step(t):
         sim.update_E([])
         sim.E[ind] += numpy.float32(wl["wave"](t))
+        if mon_idx is not None:
+            x = numpy.asarray(sim.E).reshape(-1)[mon_idx].astype(numpy.float64)
+            acc[:] += x[:, None] * numpy.exp(-1j * om[None, :] * (t + 1) * dt)
         sim.update_H([])
         if kw.get("do_poynting", True):
             sim.update_S([])
@@ -217,8 +261,10 @@ def run_reference(args):
         "ms_per_step": round(1e3 * numpy.prod(wl["shape"]) / (res["value"] * 1e6), 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
-        "config": {"workload": wl["describe"], "grid": list(wl["shape"]),
-                   "timed_steps_run": res["sample"]},
+        "config": workload_config(wl, workloads.face_cells(wl["shape"], wl["kwargs"]["pmls"]), 4,
+                                  wl["kwargs"].get("do_poynting", True)),
+        "path": "the reference's own kernels (rendered OpenCL C) stepping the grid on the host cores"
+                + ("; E at the monitor points transformed in float64 every step" if wl["name"] == "c2" else ""),
         "cpu_baseline": {"value": round(res["value"], 3), "unit": UNIT, "cores": nthreads,
                          "kind": res["kind"], "sample": res["sample"]},
         "e2e": {"value": round(res["value"], 3), "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -278,9 +324,10 @@ def time_dropin(sim, lib, wave_dev, ind, K, W, poynting, world):
     return total, per
 
 
-def time_run(sim, lib, wave_dev, ind, K, W, world, mode):
+def time_run(sim, lib, wave_dev, ind, K, W, world, mode, monitor=None):
     """K steps in one fdtd_run call bracketed by CUDA events. mode: 'hs' (E in place, H and S
-    in one launch), 'fused' (one kernel per step) or None (the per-update kernels)."""
+    in one launch), 'fused' (one kernel per step) or None (the per-update kernels); monitor: a
+    DftMonitor sampled after every timed step (inside the timed region)."""
     import torch
     from opencl_fdtd_gb300 import _lib
     stream = sim.queue
@@ -301,9 +348,12 @@ def time_run(sim, lib, wave_dev, ind, K, W, world, mode):
             replicas.barrier()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        mon = ctypes.byref(monitor.struct(K)) if monitor is not None else None
         e0.record(stream)
-        _lib.check(lib.fdtd_run(sim._plan, ctypes.byref(bufs), st, K, ctypes.byref(timed), None))
+        _lib.check(lib.fdtd_run(sim._plan, ctypes.byref(bufs), st, K, ctypes.byref(timed), mon))
         e1.record(stream)
+        if monitor is not None:
+            monitor.samples += K
         torch.cuda.synchronize()
         if world > 1:
             from opencl_fdtd_gb300 import replicas
@@ -333,6 +383,91 @@ def run_kernel_ms(sim, lib, wave_dev, ind, steps):
     n = ctypes.c_int32()
     _lib.check(lib.fdtd_run_kernel_ms(sim._plan, ms, ctypes.byref(n)))
     return {"k_bulk_e": ms[0], "k_bulk_hs": ms[1]}, n.value
+
+
+def c2_parity(wl, steps: int):
+    """Relative L2 of the float32 run (the default Simulation.run path) against the same steps in
+    float64 on the GPU, for E, H and S."""
+    import copy
+    import torch
+    from opencl_fdtd_gb300 import Simulation
+    vals = [wl["wave"](t) for t in range(steps)]
+    g = Simulation(**copy.deepcopy(wl["kwargs"]))
+    g.run(steps, point_sources=[(wl["source_index"], vals)])
+    path = {1: "per-update", 2: "H+S", 3: "one-pass"}.get(g.tuning("last_run_path"), "?")
+    got = {k: g.get(k).astype(numpy.float64) for k in ("E", "H", "S")}
+    del g
+    kw = copy.deepcopy(wl["kwargs"])
+    kw["epsilon"] = [e.astype(numpy.float64) for e in kw["epsilon"]]
+    kw["float_type"] = numpy.float64
+    d = Simulation(**kw)
+    d.run(steps, point_sources=[(wl["source_index"], vals)])
+    err = {}
+    for k in ("E", "H", "S"):
+        ref = d.get(k)
+        err[k] = float("%.4g" % (numpy.linalg.norm(got[k] - ref) / numpy.linalg.norm(ref)))
+    del d
+    torch.cuda.empty_cache()
+    return {"steps": steps, "path": path, "rel_l2_vs_fp64": err,
+            "reference": "the same steps in float64 on the GPU (bit-identical to the float64 oracle in the "
+                         "GPU tests); float32 bit-identical to the oracle (tests/test_gpu_config2.py)"}
+
+
+def run_extras(args, wl):
+    """Bounded versions of the other halves of the metric, for the default run: the float64
+    error of the benchmarked workload, the batched sweep (a subset of c4's variants and steps)
+    and the learned thin boundary (fewer teacher runs than c5 states)."""
+    import torch
+    out = {}
+    t0 = time.perf_counter()
+    out["parity"] = c2_parity(wl, args.parity_steps) if wl["name"] == "c2" else None
+    t1 = time.perf_counter()
+    b = c4_measure(args.extras_variants, args.extras_steps, 100 if args.extras_steps % 100 == 0 else args.extras_steps,
+                   storages=("f32", "bf16u"))
+    torch.cuda.empty_cache()
+    cfg = b["config"]
+    out["batched"] = {
+        "workload": "c4 subset: the first %d of c4's seeded L3 variants, %d steps each, f32 arithmetic"
+                    % (cfg["variants"], cfg["steps"]),
+        "cells": cfg["cells"], "interior_cells": cfg["interior_cells"],
+        "plain": {"value": b["plain"]["value"], "interior_value": b["plain"]["interior_value"],
+                  "ms": b["plain"]["ms"], "error_vs_f64": b["plain"]["error_vs_f64"],
+                  "path": "per-variant Simulation.run (per-update kernels)"},
+        "f32": {k: b["batched"]["f32"][k] for k in ("value", "interior_value", "ms", "error_vs_f64",
+                                                    "rel_l2_E_vs_plain_f32", "bit_identical_to_plain")},
+        "bf16u": {k: b["batched"]["bf16u"][k] for k in ("value", "interior_value", "ms", "error_vs_f64",
+                                                        "rel_l2_E_vs_plain_f32")},
+        "schedule": b["batched"]["f32"]["tiles"]["schedule"],
+        "speedup_f32_vs_plain": round(b["plain"]["ms"] / b["batched"]["f32"]["ms"], 3),
+        "speedup_bf16u_vs_plain": round(b["plain"]["ms"] / b["batched"]["bf16u"]["ms"], 3),
+        "unit": UNIT}
+    for k in ("f32", "bf16u"):
+        e = out["batched"][k]["error_vs_f64"]
+        out["batched"][k]["error_vs_f64"] = {"rel_l2_E": e["rel_l2_E"], "dft_peak_rel": e["dft_peak_rel"]}
+    t2 = time.perf_counter()
+    c = c5_measure(args.learned_runs, args.learned_steps)
+    torch.cuda.empty_cache()
+    pick = c["verdicts"][c["candidate_timed"]]
+    out["learned"] = {
+        "workload": "c5 at %d teacher runs (c5 states 200): the c2 cavity with a 2-cell learned layer on "
+                    "every face or on the z faces, against its 8-cell CPML, %d steps" % (args.learned_runs,
+                                                                                     args.learned_steps),
+        "deployed": c["deployed"], "candidate": c["candidate_timed"],
+        "useful_interior_value": c["value"], "unit": UNIT,
+        "plain_cpml8_useful_value": c["plain_cpml8"]["useful_mcells_per_s"],
+        "thin_all_faces": {"useful_value": c["thin_learned"]["useful_mcells_per_s"],
+                           "interior_rel_l2_vs_plain_cpml8": c["thin_learned"]["interior_rel_l2_vs_plain_cpml8"],
+                           "reflection_db": pick.get("reflection_db"), "accepted": pick.get("accepted")},
+        "thin_z_faces": {"useful_value": c["thin_z_learned"]["useful_mcells_per_s"],
+                         "interior_rel_l2_vs_plain_cpml8": c["thin_z_learned"]["interior_rel_l2_vs_plain_cpml8"],
+                         "reflection_db": c["thin_z_learned"]["verdict"].get("reflection_db"),
+                         "accepted": c["thin_z_learned"]["verdict"].get("accepted")},
+        "target": "reflection <= -40 dB and interior relative L2 <= 1e-3 against the plain 8-cell CPML run; "
+                  "CPML is deployed otherwise",
+        "predict_roofline": c["roofline"]}
+    t3 = time.perf_counter()
+    out["extras_seconds"] = {"parity": round(t1 - t0, 1), "batched": round(t2 - t1, 1), "learned": round(t3 - t2, 1)}
+    return out
 
 
 def main():
@@ -383,14 +518,16 @@ def main():
     res = {}
     if args.path in ("dropin", "default", "all"):
         res["dropin"] = time_dropin(sim, lib, wave_dev, ind, K, W, poynting, world)
+    mon = sim.dft_monitor(monitor_points(wl), monitor_omegas(), record=False) if wl["name"] == "c2" else None
     if args.path in ("hs", "default", "all") and poynting:
-        res["hs"] = time_run(sim, lib, wave_dev, ind, K, W, world, "hs")
+        res["hs"] = time_run(sim, lib, wave_dev, ind, K, W, world, "hs", monitor=mon)
         hs_per = run_kernel_ms(sim, lib, wave_dev, ind, min(W + K, 640))
     if args.path in ("slab", "all"):
         res["slab"] = time_run(sim, lib, wave_dev, ind, K, W, world, None)
         sim.tune(slab=0)
     if args.path in ("fused", "all"):
-        res["fused"] = time_run(sim, lib, wave_dev, ind, K, W, world, "fused")
+        res["fused"] = time_run(sim, lib, wave_dev, ind, K, W, world, "fused",
+                                monitor=mon if args.path == "fused" else None)
     clock = clocks.stop()
 
     from opencl_fdtd_gb300 import replicas
@@ -459,9 +596,22 @@ def main():
         e2e = run_e2e(sim, wl, args.e2e_steps, world, run_api=(head != "dropin"),
                       path={"fused": "fused", "hs": "hs", "slab": "plain"}.get(head, "auto"))
 
+    mon_out = None
+    if mon is not None and mon.samples:
+        acc = mon.accum.cpu().numpy()
+        mag = numpy.hypot(acc[..., 0], acc[..., 1])
+        mon_out = {"points": len(MONITOR_OFFSETS), "frequencies": len(monitor_omegas()), "samples": mon.samples,
+                   "in_timed_region": True, "centre_abs_dft": [float("%.6g" % v) for v in mag[0]]}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(wl, args.cpu_seconds, os.cpu_count() or 1)
+
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras:
+        del sim
+        torch.cuda.empty_cache()
+        extras = run_extras(args, wl)
 
     if rank == 0:
         out = {
@@ -469,15 +619,13 @@ def main():
             "steps": K, "warmup": W, "ms_per_step": round(hp["ms_per_step"], 5),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded L3 cavity geometry and source)",
-            "config": {"workload": wl["describe"], "grid": list(wl["shape"]), "cells": N,
-                       "cpml_face_cells": fc,
-                       "path": {"fused": "Simulation.run(path='fused'): one fused E+source+H+S kernel per step",
+            "config": workload_config(wl, fc, elem, poynting),
+            "path": {"fused": "Simulation.run(path='fused'): one fused E+source+H+S kernel per step",
                                 "hs": "Simulation.run: E in place, point source, H+S in one launch (H ping-pong)",
                                 "slab": "Simulation.run(path='plain'): E, point source, H, S update kernels",
                                 "dropin": "per-call update_E / source add / update_H / update_S"}[head],
-                       "l2": "inputs (~%.0f MB of fields) larger than the 129 MB L2; no flush"
-                             % (sim.E.numel() * elem * (6 if poynting else 3) / 1e6),
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "monitor": mon_out,
             # the dominant kernel's roofline: per-call timing of the same kernels the run
             # path launches (the fused path reports its own kernel)
             # the dominant kernel of the headline path, timed per launch with CUDA events
@@ -493,6 +641,7 @@ def main():
                           "roofline_frac": v["roofline"]["frac"], "kernel": v["roofline"]["kernel"]}
                       for k, v in out_paths.items()},
         }
+        out.update(extras)
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -575,20 +724,18 @@ def _peak_frequency(series, dt, w0):
     return float(w[k])
 
 
-def run_c4(args):
+def c4_measure(n_variants: int, steps: int, chunk: int, storages=("f32", "bf16", "fp16", "bf16u")):
     """Batched sweep: per-variant Simulation.run against one persistent launch per chunk of
-    steps (CUDA graph replays, autotuned tiles) in float32, bfloat16 and float16 storage; the
-    16-bit errors against a float64 run of every variant (relative L2 of E, DFT-peak
-    frequency of the centre E_y series)."""
+    steps (CUDA graph replays, autotuned tiles) in float32 and 16-bit storage; every storage's
+    errors against a float64 run of every variant (relative L2 of E, DFT-peak frequency of the
+    centre E_y series). Returns the plain and batched timings, the errors and the setup."""
     import torch
     from opencl_fdtd_gb300 import Simulation, workloads
     from opencl_fdtd_gb300.batch import BatchSimulation
-    torch.cuda.set_device(0)
-    steps, chunk = args.c4_steps, args.c4_chunk
     if steps % chunk:
-        raise SystemExit("--c4-steps must be a multiple of --c4-chunk")
+        raise SystemExit("the c4 step count must be a multiple of the chunk")
     t_setup = time.perf_counter()
-    variants = workloads.c4(n=args.c4_variants, steps=steps)
+    variants = workloads.c4(n=n_variants, steps=steps)
     kws, idx = [], []
     for var in variants:
         kw, ind = workloads.c4_kwargs(var)
@@ -639,7 +786,7 @@ def run_c4(args):
     plain_E = [s.E.clone() for s in sims]
     plain_series = [m.series()[:, 0] for m in mons]
     results = {}
-    for storage in ("f32", "bf16", "fp16", "bf16u"):
+    for storage in storages:
         reset()
         b = BatchSimulation(sims, storage=storage, sources=sources, monitors=monitors, steps=steps)
         tune = b.autotune(steps=10)
@@ -662,7 +809,7 @@ def run_c4(args):
         numpy.array_equal(a, c) for a, c in zip(plain_series, results["f32"]["series"]))
     # float64 reference of every variant: errors of the float32 and 16-bit runs
     w0 = 2 * math.pi * 40.0 / 1550.0
-    err = {k: {"rel_l2": [], "peak_rel": []} for k in ("f32", "bf16", "fp16", "bf16u")}
+    err = {k: {"rel_l2": [], "peak_rel": []} for k in storages}
     for v, var in enumerate(variants):
         kw64, ind = workloads.c4_kwargs(var, float_type=numpy.float64)
         s64 = Simulation(**kw64)
@@ -677,6 +824,18 @@ def run_c4(args):
             err[k]["rel_l2"].append(float(torch.linalg.norm((e - ref)[fin]) / nref))
             err[k]["peak_rel"].append(abs(_peak_frequency(results[k]["series"][v], s64.dt, w0) - w_ref) / w_ref)
         del s64, m64, ref
+    # plain (per-variant) float32 against float64: the error every batched storage adds to
+    plain_err = []
+    for v, var in enumerate(variants):
+        kw64, ind = workloads.c4_kwargs(var, float_type=numpy.float64)
+        s64 = Simulation(**kw64)
+        s64.run(steps, point_sources=[(ind, wave)], path="plain")
+        ref = s64.E
+        fin = torch.isfinite(ref)
+        plain_err.append(float(torch.linalg.norm((plain_E[v].double() - ref)[fin]) / torch.linalg.norm(ref[fin])))
+        del s64, ref
+    out["plain"]["error_vs_f64"] = {"rel_l2_E": {"median": float(numpy.median(plain_err)),
+                                                  "max": float(numpy.max(plain_err))}}
     for k in err:
         a = numpy.array(err[k]["rel_l2"])
         p = numpy.array(err[k]["peak_rel"])
@@ -685,6 +844,22 @@ def run_c4(args):
             "dft_peak_rel": {"median": float(numpy.median(p)), "max": float(p.max())},
             "per_variant_rel_l2_E": [float("%.3g" % x) for x in a],
             "per_variant_dft_peak_rel": [float("%.3g" % x) for x in p]}
+        # against the plain per-variant float32 run
+        d = [float(torch.linalg.norm((results[k]["E"][v] - plain_E[v]).double()) /
+                   torch.linalg.norm(plain_E[v].double())) for v in range(len(variants))]
+        out["batched"][k]["rel_l2_E_vs_plain_f32"] = {"median": float(numpy.median(d)), "max": float(max(d))}
+    out["config"] = {"variants": len(variants), "steps": steps, "cells": cells, "interior_cells": interior,
+                     "setup_s": round(setup_s, 1), "steps_per_graph": chunk}
+    return out
+
+
+def run_c4(args):
+    """The batched sweep of c4 at its stated size, as one JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    steps, chunk = args.c4_steps, args.c4_chunk
+    out = c4_measure(args.c4_variants, steps, chunk)
+    cells, interior = out["config"]["cells"], out["config"]["interior_cells"]
     best = out["batched"]["f32"]
     line = {
         "metric": METRIC, "value": best["value"], "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": 10,
@@ -692,8 +867,8 @@ def run_c4(args):
         "vs_baseline": None, "dtype": "f32 arithmetic; f32 / bf16 / fp16 / bf16 (no tile exponents) storage", "data": "synthetic (seeded L3 variants)",
         "config": {"workload": "c4: %d seeded L3-cavity variants, grids U{96..256}xU{96..224}xU{48..73}, "
                                "a ~ U[8,12], r ~ U[0.25a,0.35a], 8-cell CPML x6, Poynting off, %d steps"
-                               % (len(variants), steps),
-                   "cells": cells, "interior_cells": interior, "setup_s": round(setup_s, 1),
+                               % (out["config"]["variants"], steps),
+                   "cells": cells, "interior_cells": interior, "setup_s": out["config"]["setup_s"],
                    "l2": "inputs (%.1f GB of fields) larger than the 129 MB L2; no flush" % (cells * 36 / 1e9)},
         "plain": out["plain"], "batched": out["batched"],
         "speedup_batched_f32_vs_plain": round(out["plain"]["ms"] / best["ms"], 3),
@@ -758,7 +933,7 @@ def run_c3(args):
     print(json.dumps(line), flush=True)
 
 
-def run_c5(args):
+def c5_measure(runs: int, K: int):
     """Learned thin boundary on the c2 cavity: teacher data (Mur-memory targets), candidate
     networks (least squares on Mur's stencil, least squares shrunk towards Mur's map at two
     strengths, and Mur's map itself),
@@ -772,7 +947,7 @@ def run_c5(args):
     from opencl_fdtd_gb300 import learned_boundary as L
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
-    data = L.make_teacher_data(runs=args.c5_runs, seed=5, memory=L.MUR_MEMORY)
+    data = L.make_teacher_data(runs=runs, seed=5, memory=L.MUR_MEMORY)
     torch.cuda.synchronize()
     data_s = time.perf_counter() - t0
     probe = L.BoundaryNet(seed=6, memory=L.MUR_MEMORY)
@@ -817,7 +992,6 @@ def run_c5(args):
     rel = {name: r for name, (_, r) in cands.items()}
 
     # the c2 cavity: plain with its CPML, and cut to the useful interior plus the 2-cell layer
-    K = args.c5_steps
     wl = workloads.c2()
     kw = dict(wl["kwargs"])
     shape = wl["shape"]
@@ -941,7 +1115,7 @@ def run_c5(args):
                                                                       "x".join(map(str, useful)),
                                                                       "x".join(map(str, thin_shape)), K),
                    "teacher": "%d runs at 128^3, 16-cell CPML, 1500 steps, 1-8 spheres eps U[1,12] inside "
-                              "the box, dipole pulse period U[10,30] steps, random polarisation" % args.c5_runs,
+                              "the box, dipole pulse period U[10,30] steps, random polarisation" % runs,
                    "l2": "c2 fields (%.0f MB) larger than the 129 MB L2; no flush" % (int(numpy.prod(shape)) * 36 / 1e6)},
         "deployed": deployed, "candidate_timed": pick,
         "verdicts": {name: {k: (round(v, 2) if isinstance(v, float) and math.isfinite(v) else
@@ -974,7 +1148,12 @@ def run_c5(args):
                                                "of one bf16 pass)"},
         "gpu_launches": "thin: 4 + the plain step's per step; plain: the plain step's",
     }
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_c5(args):
+    """The learned thin boundary of c5 at its stated teacher-run count, as one JSON line."""
+    print(json.dumps(c5_measure(args.c5_runs, args.c5_steps)), flush=True)
 
 
 if __name__ == "__main__":
