@@ -2,9 +2,11 @@
 //
 // All variants' work is cut into tiles of BATCH_THREADS consecutive (y, z) cells times a chunk
 // of x planes. Two schedules run the same tile code:
-//   * persistent: a cooperative grid of a few blocks per SM loops over the tile list of every
-//     variant for the E half-step, synchronises the grid, does the same for the H half-step,
-//     synchronises again, and repeats -- one launch advances the whole sweep by nsteps steps;
+//   * persistent: a cooperative grid of two blocks per SM takes the tiles of every variant
+//     from a device work counter for the E half-step, synchronises the grid, does the same for
+//     the H half-step, synchronises again, and repeats -- one launch advances the whole sweep by
+//     nsteps steps (two blocks: the E and H tile bodies together need 128 registers without
+//     spilling; at three blocks per SM they spill and run slower);
 //   * per half-step: one launch of one block per tile for E, one for H, per step (captured in
 //     a CUDA graph by the caller); the hardware scheduler then overlaps blocks.
 // Either way there is no per-variant launch or tail. Point sources are added and monitor
@@ -469,24 +471,48 @@ __device__ void batch_h_tile(const BVar &v, int4 tl)
 }
 
 template <int ST>
+__device__ __forceinline__ void batch_e_item(const BatchK &k, uint32_t ti, int64_t step)
+{
+    const int4 tl = k.tiles[ti];
+    batch_e_tile<ST>(k.vars[tl.x], tl, step, k.rows);
+}
+
+template <int ST>
+__device__ __forceinline__ void batch_h_item(const BatchK &k, uint32_t ti)
+{
+    const int4 tl = k.tiles[ti];
+    batch_h_tile<ST>(k.vars[tl.x], tl);
+}
+
+// next tile of the half-step whose counter is `ctr` (>= ntiles: none left)
+__device__ __forceinline__ uint32_t next_tile(uint32_t *ctr, uint32_t *slot)
+{
+    __syncthreads();                                     // every thread has read the last one
+    if (threadIdx.x == 0) *slot = atomicAdd(ctr, 1u);
+    __syncthreads();
+    return *slot;
+}
+
+template <int ST>
 __global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(const BatchK k)
 {
+    __shared__ uint32_t item;
     cg::grid_group grid = cg::this_grid();
     const int64_t step0 = *k.step;
     for (int t = 0; t < k.nsteps; ++t) {
         const int64_t step = step0 + t;
-        for (uint32_t ti = blockIdx.x; ti < k.ntiles; ti += gridDim.x) {
-            const int4 tl = k.tiles[ti];
-            batch_e_tile<ST>(k.vars[tl.x], tl, step, k.rows);
-        }
+        // half-step 2t uses counter 0, 2t + 1 counter 1; a counter is cleared right after the
+        // grid barrier that ends its half-step, two barriers before its next use
+        for (uint32_t ti = next_tile(&k.work[0], &item); ti < k.ntiles; ti = next_tile(&k.work[0], &item))
+            batch_e_item<ST>(k, ti, step);
         grid.sync();
-        for (uint32_t ti = blockIdx.x; ti < k.ntiles; ti += gridDim.x) {
-            const int4 tl = k.tiles[ti];
-            batch_h_tile<ST>(k.vars[tl.x], tl);
-        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) k.work[0] = 0u;
+        for (uint32_t ti = next_tile(&k.work[1], &item); ti < k.ntiles; ti = next_tile(&k.work[1], &item))
+            batch_h_item<ST>(k, ti);
         grid.sync();
+        if (blockIdx.x == 0 && threadIdx.x == 0) k.work[1] = 0u;
     }
-    // every block read the counter before its first grid barrier
+    // every block read the step counter before its first grid barrier
     if (blockIdx.x == 0 && threadIdx.x == 0) *k.step = step0 + k.nsteps;
 }
 

@@ -57,6 +57,8 @@ struct BatchK {
     int32_t nsteps;
     int64_t *step;              // device step counter: read at start, advanced by nsteps at end
     int64_t rows;               // rows of the source and series arrays
+    uint32_t *work;             // persistent schedule: tiles handed out so far in the current
+                                // half-step, two counters used alternately (zero between launches)
 };
 
 template <int ST>

@@ -26,6 +26,7 @@ struct FdtdBatch {
     int4 *tiles = nullptr;       // device tile list
     uint32_t ntiles = 0;
     int64_t *step = nullptr;     // device step counter
+    uint32_t *work = nullptr;    // persistent schedule's two tile counters
 };
 
 namespace {
@@ -177,6 +178,8 @@ int fdtd_batch_create(const FdtdBatchVariant *vars, int32_t n, int32_t storage, 
                         "copy batch variants");
     if (!rc) rc = check_cuda(cudaMalloc(&b->step, sizeof(int64_t)), "cudaMalloc(batch step)");
     if (!rc) rc = check_cuda(cudaMemset(b->step, 0, sizeof(int64_t)), "clear batch step");
+    if (!rc) rc = check_cuda(cudaMalloc(&b->work, 2 * sizeof(uint32_t)), "cudaMalloc(batch work counters)");
+    if (!rc) rc = check_cuda(cudaMemset(b->work, 0, 2 * sizeof(uint32_t)), "clear batch work counters");
     if (!rc) rc = build_tiles(b);
     if (rc) {
         fdtd_batch_destroy(b);
@@ -192,6 +195,7 @@ int fdtd_batch_destroy(FdtdBatch *b)
     if (b->vars) cudaFree(b->vars);
     if (b->tiles) cudaFree(b->tiles);
     if (b->step) cudaFree(b->step);
+    if (b->work) cudaFree(b->work);
     delete b;
     return FDTD_OK;
 }
@@ -227,6 +231,7 @@ int fdtd_batch_run(FdtdBatch *b, void *stream, int32_t nsteps)
     k.nsteps = nsteps;
     k.step = b->step;
     k.rows = b->rows;
+    k.work = b->work;
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e;
     if (b->schedule == FDTD_BATCH_LAUNCHES) {

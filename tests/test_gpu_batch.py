@@ -210,3 +210,30 @@ def test_autotune_restores_state_and_caches(tmp_path):
         assert torch.equal(sa, sb)
     again = b.autotune(steps=2, cache_path=cache, xchunks=(2, 8), blocks=(1, 2))
     assert again["cached"] and again["xchunk"] == choice["xchunk"]
+
+
+@pytest.mark.parametrize("schedule", ["launches", "persistent"])
+def test_batch_f32_variant_equals_oracle(schedule):
+    """One variant of the batch stepped by the batched kernels against the oracle's per-call
+    loop (update_E, the sources added in list order, update_H) bit for bit."""
+    import os
+    from oracle import port
+    from opencl_fdtd_gb300.batch import BatchSimulation
+    kws = [_variant(s, T, 30 + i) for i, (s, T) in enumerate(SHAPES[:3])]
+    n = 11
+    got = _sims(kws)
+    src = _sources(got, n, 7)
+    b = BatchSimulation(got, storage="f32", sources=src, monitors=None, steps=n)
+    b.tune(4, 0, schedule)
+    b.run(n)
+    torch.cuda.synchronize()
+    for v in (0, 2):
+        c = port.PortSimulation(nthreads=os.cpu_count(), **copy.deepcopy(kws[v]))
+        for t in range(n):
+            c.update_E()
+            for ind, vals in src[v]:
+                c.E[ind] = c.E[ind] + numpy.float32(vals[t])
+            c.update_H()
+        for k in ("E", "H"):
+            x = getattr(got[v], k).detach().cpu().numpy().reshape(-1)
+            assert numpy.array_equal(x, getattr(c, k).reshape(-1)), (v, k)
