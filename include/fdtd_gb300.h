@@ -255,9 +255,11 @@ int fdtd_count_nonfinite(FdtdPlan *plan, const FdtdBuffers *buf, uint32_t *count
 
 /* Run nsteps canonical steps (fdtd.py:162-175: E, F, point sources, H, G, S) on the stream
  * with no host round trip. src and mon may be NULL; mon is sampled after every step and its
- * step / series_row advance by nsteps. With the scratch buffers set (and no Bloch
- * boundaries, at most 8 sources, no overlapping CPML faces) each step is one fused kernel;
- * oS is then written on the last step only. */
+ * step / series_row advance by nsteps. With the second copies of FdtdBuffers set (and no
+ * Bloch boundaries, at most 8 sources, no overlapping CPML faces) each step is two launches
+ * (H2 and psi_h2: update_E in place, then H and S) or one (E2, H2 and every psi copy: the
+ * one-pass step); oS is then written on the last step only. The path taken is read back with
+ * fdtd_plan_get(FDTD_GET_LAST_RUN_PATH). */
 int fdtd_run(FdtdPlan *plan, const FdtdBuffers *buf, void *stream, int32_t nsteps,
              const FdtdPointSources *src, FdtdDftMonitor *mon);
 

@@ -106,15 +106,24 @@ __global__ void k_lbc_gather(const LGrid g, const float *E, const float *H, floa
 }
 
 // ---- training: forward (float32), one thread per sample ---------------------------------------
+// Dynamic shared memory of the float32 MLP kernels: the parameters, then one column of 64
+// hidden activations per thread, stored k-major (hs[k * T + t]) so that the runtime loops over
+// k read them without bank conflicts and every register array keeps compile-time indices (a
+// hidden vector indexed by the runtime k would live in local memory).
+constexpr size_t MLP32_SMEM = ((size_t)LBC_NPARAM + (size_t)LBC_HID * 128) * sizeof(float);
+static_assert(T_FWD == 128, "MLP32_SMEM holds 128 hidden columns");
+
 __global__ void __launch_bounds__(T_FWD) k_mlp_fwd(const float *P, const float *X, int B, float *Y, float *A1,
                                                     float *A2, float *H1, float *H2)
 {
-    __shared__ float w[LBC_NPARAM];
+    extern __shared__ float mlp_smem[];
+    float *const w = mlp_smem;
+    float *const hs = mlp_smem + LBC_NPARAM + threadIdx.x;   // hs[k * T_FWD]: this thread's column
     for (int i = threadIdx.x; i < LBC_NPARAM; i += blockDim.x) w[i] = P[i];
     __syncthreads();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= B) return;
-    float h[LBC_HID], a[LBC_HID];
+    float a[LBC_HID];
 #pragma unroll
     for (int j = 0; j < LBC_HID; ++j) a[j] = w[LBC_B1 + j];
     for (int k = 0; k < LBC_IN; ++k) {
@@ -125,29 +134,34 @@ __global__ void __launch_bounds__(T_FWD) k_mlp_fwd(const float *P, const float *
 #pragma unroll
     for (int j = 0; j < LBC_HID; ++j) {
         A1[(uint64_t)r * LBC_HID + j] = a[j];
-        h[j] = gelu(a[j]);
-        H1[(uint64_t)r * LBC_HID + j] = h[j];
+        const float hj = gelu(a[j]);
+        hs[j * T_FWD] = hj;
+        H1[(uint64_t)r * LBC_HID + j] = hj;
     }
 #pragma unroll
     for (int j = 0; j < LBC_HID; ++j) a[j] = w[LBC_B2 + j];
     for (int k = 0; k < LBC_HID; ++k) {
-        const float hk = h[k];
+        const float hk = hs[k * T_FWD];
 #pragma unroll
         for (int j = 0; j < LBC_HID; ++j) a[j] += hk * w[LBC_W2 + k * LBC_HID + j];
     }
 #pragma unroll
     for (int j = 0; j < LBC_HID; ++j) {
         A2[(uint64_t)r * LBC_HID + j] = a[j];
-        h[j] = gelu(a[j]);
-        H2[(uint64_t)r * LBC_HID + j] = h[j];
+        const float hj = gelu(a[j]);
+        hs[j * T_FWD] = hj;
+        H2[(uint64_t)r * LBC_HID + j] = hj;
+    }
+    float y[LBC_OUT];
+#pragma unroll
+    for (int o = 0; o < LBC_OUT; ++o) y[o] = w[LBC_B3 + o];
+    for (int k = 0; k < LBC_HID; ++k) {
+        const float hk = hs[k * T_FWD];
+#pragma unroll
+        for (int o = 0; o < LBC_OUT; ++o) y[o] += hk * w[LBC_W3 + k * LBC_OUT + o];
     }
 #pragma unroll
-    for (int o = 0; o < LBC_OUT; ++o) {
-        float y = w[LBC_B3 + o];
-#pragma unroll
-        for (int k = 0; k < LBC_HID; ++k) y += h[k] * w[LBC_W3 + k * LBC_OUT + o];
-        Y[(uint64_t)r * LBC_OUT + o] = y;
-    }
+    for (int o = 0; o < LBC_OUT; ++o) Y[(uint64_t)r * LBC_OUT + o] = y[o];
 }
 
 // ---- training: backward through the activations, one thread per sample ------------------------
@@ -269,10 +283,14 @@ __global__ void k_adam(float *P, const float *G, float *M, float *V, int n, floa
 constexpr int T_APPLY = 128;
 
 // float32 weights [6 faces][LBC_NPARAM] on the CUDA cores (the checker of the bfloat16 kernel)
+static_assert(T_APPLY == 128, "MLP32_SMEM holds 128 hidden columns");
+
 __global__ void __launch_bounds__(T_APPLY) k_lbc_predict32(const LGrid g, int side, float memory, const float *W,
                                                            const float *E, const float *H, float *pred)
 {
-    __shared__ float w[LBC_NPARAM];
+    extern __shared__ float mlp_smem[];
+    float *const w = mlp_smem;
+    float *const hs = mlp_smem + LBC_NPARAM + threadIdx.x;   // hs[k * T_APPLY]: this thread's column
     // blockIdx.y: face; its columns: blockIdx.x * T_APPLY + threadIdx.x
     const int fi = blockIdx.y;
     const LFace &f = g.face[fi];
@@ -291,7 +309,7 @@ __global__ void __launch_bounds__(T_APPLY) k_lbc_predict32(const LGrid g, int si
     }
     // layer 1 is linear in the inputs: accumulate W1^T x on the raw stencil while summing its
     // squares, then scale by 1/r (the normalisation) and add the bias
-    float a[LBC_HID], h[LBC_HID];
+    float a[LBC_HID];
 #pragma unroll
     for (int j = 0; j < LBC_HID; ++j) a[j] = 0.f;
     float ss = 0.f;
@@ -323,23 +341,26 @@ __global__ void __launch_bounds__(T_APPLY) k_lbc_predict32(const LGrid g, int si
 #pragma unroll
     for (int j = 0; j < LBC_HID; ++j) a[j] = w[LBC_B1 + j] + a[j] * inv;
 #pragma unroll
-    for (int j = 0; j < LBC_HID; ++j) h[j] = gelu(a[j]);
+    for (int j = 0; j < LBC_HID; ++j) hs[j * T_APPLY] = gelu(a[j]);
 #pragma unroll
     for (int j = 0; j < LBC_HID; ++j) a[j] = w[LBC_B2 + j];
     for (int k = 0; k < LBC_HID; ++k) {
-        const float hk = h[k];
+        const float hk = hs[k * T_APPLY];
 #pragma unroll
         for (int j = 0; j < LBC_HID; ++j) a[j] += hk * w[LBC_W2 + k * LBC_HID + j];
     }
 #pragma unroll
-    for (int j = 0; j < LBC_HID; ++j) h[j] = gelu(a[j]);
+    for (int j = 0; j < LBC_HID; ++j) hs[j * T_APPLY] = gelu(a[j]);
+    float y[LBC_OUT];
 #pragma unroll
-    for (int o = 0; o < LBC_OUT; ++o) {
-        float y = w[LBC_B3 + o];
+    for (int o = 0; o < LBC_OUT; ++o) y[o] = w[LBC_B3 + o];
+    for (int k = 0; k < LBC_HID; ++k) {
+        const float hk = hs[k * T_APPLY];
 #pragma unroll
-        for (int k = 0; k < LBC_HID; ++k) y += h[k] * w[LBC_W3 + k * LBC_OUT + o];
-        out[o] = y * r + memory * out[o];
+        for (int o = 0; o < LBC_OUT; ++o) y[o] += hk * w[LBC_W3 + k * LBC_OUT + o];
     }
+#pragma unroll
+    for (int o = 0; o < LBC_OUT; ++o) out[o] = y[o] * r + memory * out[o];
 }
 
 // an exactly linear layer (LBC_LINEAR): one thread per column, 108 x 6 products, weights
@@ -752,11 +773,31 @@ cudaError_t launch_lbc_gather(const LGrid &g, const float *E, const float *H, fl
     return cudaGetLastError();
 }
 
+// The shared-memory opt-in above 48 KB is a per-device function attribute: set it once per device
+// and kernel slot (setting it twice from two threads is harmless).
+enum : int { SMEM_MLP_FWD = 0, SMEM_PREDICT32 = 1, SMEM_MMA = 2, SMEM_MMA_SPLIT = 3, SMEM_SLOTS = 4 };
+
+static cudaError_t smem_opt_in(const void *fn, int slot, size_t bytes)
+{
+    constexpr int MAX_DEV = 64;
+    static bool set[MAX_DEV][SMEM_SLOTS] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < MAX_DEV && set[dev][slot]) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < MAX_DEV) set[dev][slot] = true;
+    return cudaSuccess;
+}
+
 cudaError_t launch_mlp_fwd(const float *P, const float *X, int B, float *Y, float *A1, float *A2, float *H1,
                            float *H2, cudaStream_t st)
 {
     if (B <= 0) return cudaSuccess;
-    k_mlp_fwd<<<(B + T_FWD - 1) / T_FWD, T_FWD, 0, st>>>(P, X, B, Y, A1, A2, H1, H2);
+    const cudaError_t e = smem_opt_in((const void *)k_mlp_fwd, SMEM_MLP_FWD, MLP32_SMEM);
+    if (e != cudaSuccess) return e;
+    k_mlp_fwd<<<(B + T_FWD - 1) / T_FWD, T_FWD, MLP32_SMEM, st>>>(P, X, B, Y, A1, A2, H1, H2);
     return cudaGetLastError();
 }
 
@@ -832,24 +873,19 @@ cudaError_t launch_lbc_predict(const LGrid &g, int side, int precision, float me
     for (int f = 0; f < g.nface; ++f) maxc = g.face[f].ncol > maxc ? g.face[f].ncol : maxc;
     if (precision == LBC_F32 || precision == LBC_LINEAR) {
         const dim3 gi((maxc + T_APPLY - 1) / T_APPLY, (unsigned)g.nface, 1);
-        if (precision == LBC_F32) k_lbc_predict32<<<gi, T_APPLY, 0, st>>>(g, side, memory, (const float *)W, E, H, pred);
-        else k_lbc_predict_lin<<<gi, T_APPLY, 0, st>>>(g, side, memory, (const float *)W, E, H, pred);
+        if (precision == LBC_F32) {
+            const cudaError_t e = smem_opt_in((const void *)k_lbc_predict32, SMEM_PREDICT32, MLP32_SMEM);
+            if (e != cudaSuccess) return e;
+            k_lbc_predict32<<<gi, T_APPLY, MLP32_SMEM, st>>>(g, side, memory, (const float *)W, E, H, pred);
+        } else {
+            k_lbc_predict_lin<<<gi, T_APPLY, 0, st>>>(g, side, memory, (const float *)W, E, H, pred);
+        }
         return cudaGetLastError();
     }
-    // the shared-memory opt-in is a per-device function attribute: set it once per device
-    // (setting it twice from two threads is harmless)
-    constexpr int MAX_DEV = 64;
-    static bool attr_set[MAX_DEV][2] = {};
     const int split = precision == LBC_BF16X2 ? 1 : 0;
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    const cudaError_t e = split ? smem_opt_in((const void *)k_lbc_predict_mma<true>, SMEM_MMA_SPLIT, MMA_SMEM)
+                                : smem_opt_in((const void *)k_lbc_predict_mma<false>, SMEM_MMA, MMA_SMEM);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= MAX_DEV || !attr_set[dev][split]) {
-        e = split ? cudaFuncSetAttribute(k_lbc_predict_mma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MMA_SMEM)
-                  : cudaFuncSetAttribute(k_lbc_predict_mma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MMA_SMEM);
-        if (e != cudaSuccess) return e;
-        if (dev >= 0 && dev < MAX_DEV) attr_set[dev][split] = true;
-    }
     const dim3 gi((maxc + MMA_COLS - 1) / MMA_COLS, (unsigned)g.nface, 1);
     if (split)
         k_lbc_predict_mma<true><<<gi, MMA_WARPS * 32, MMA_SMEM, st>>>(g, side, memory, (const uint32_t *)W, E, H, pred);
