@@ -424,23 +424,37 @@ constexpr int PK_B3 = PK_B2 + LBC_HID;            // float [8]
 static_assert(PK_B3 + 8 == LBC_PACK_WORDS, "packed layout size");
 
 constexpr int MMA_WARPS = 4;
-constexpr int MMA_TILES = 4;                      // 16-column tiles per warp per block
-constexpr int MMA_COLS = MMA_WARPS * MMA_TILES * 16;
 constexpr int XS = 120;                           // float row stride of a warp's stencil tile
 
+// two floats rounded to bfloat16 in one conversion (lo in the low half)
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 {
-    const uint32_t l = __bfloat16_as_ushort(__float2bfloat16_rn(lo));
-    const uint32_t h = __bfloat16_as_ushort(__float2bfloat16_rn(hi));
-    return l | (h << 16);
+    const __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&p);
 }
 
 // x = hi + lo with hi = bf16(x), lo = bf16(x - hi): about 16 significant bits in two bf16 parts
 __device__ __forceinline__ void split_bf16(float x0, float x1, uint32_t &hi, uint32_t &lo)
 {
-    const __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
-    hi = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-    lo = pack_bf16(x0 - __bfloat162float(h0), x1 - __bfloat162float(h1));
+    hi = pack_bf16(x0, x1);
+    const float h0 = __uint_as_float(hi << 16), h1 = __uint_as_float(hi & 0xffff0000u);
+    lo = pack_bf16(x0 - h0, x1 - h1);
+}
+
+// GELU of the tensor-core inference: erf by Abramowitz & Stegun, Handbook of Mathematical
+// Functions, formula 7.1.26 (Hastings' rational approximation, |error| <= 1.5e-7 for all x),
+// with the exponential and reciprocal on the special-function unit; well inside the bfloat16
+// (and split-bfloat16) precision of the layer inputs it feeds. Training and the float32 checker
+// use erff.
+__device__ __forceinline__ float gelu_mma(float x)
+{
+    const float z = x * 0.70710678118654752f;
+    const float az = fabsf(z);
+    const float t = __fdividef(1.0f, fmaf(0.3275911f, az, 1.0f));
+    const float poly = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f),
+                                        -0.284496736f), 0.254829592f);
+    const float e = copysignf(1.0f - poly * __expf(-az * az), z);
+    return 0.5f * x * (1.0f + e);
 }
 
 __device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1)
@@ -490,7 +504,7 @@ __device__ __forceinline__ void act_to_a(const float acc[8][4], uint32_t ah[4][4
 #pragma unroll
         for (int half = 0; half < 2; ++half) {
             const float *c = acc[2 * ks + half];
-            const float g0 = gelu(c[0]), g1 = gelu(c[1]), g2 = gelu(c[2]), g3 = gelu(c[3]);
+            const float g0 = gelu_mma(c[0]), g1 = gelu_mma(c[1]), g2 = gelu_mma(c[2]), g3 = gelu_mma(c[3]);
             if (SPLIT) {
                 split_bf16(g0, g1, ah[ks][2 * half], al[ks][2 * half]);
                 split_bf16(g2, g3, ah[ks][2 * half + 1], al[ks][2 * half + 1]);
@@ -501,53 +515,100 @@ __device__ __forceinline__ void act_to_a(const float acc[8][4], uint32_t ah[4][4
         }
 }
 
+// A warp's job: a tile of MMA_TU x 16 columns of one face (MMA_TU rows along u, 16 columns along
+// v). The cells its stencils read, (MMA_TU + 2) x 18 positions x 2 depths x 6 components, are
+// staged once in shared memory, plane (component q, depth d) by plane with a stride of
+// MMA_PL floats (MMA_PL = 16 mod 32, so the two depths a lane pair reads fall in different
+// banks), before the columns are evaluated 16 at a time. The loads follow the memory order:
+// along z (v) on x and y faces, over the depth pair z = 0, 1 (or s - 1, s - 2) first on z faces.
+constexpr int MMA_TU = 4;
+constexpr int MMA_SU = MMA_TU + 2, MMA_SV = 16 + 2;
+constexpr int MMA_PL = 112;
+static_assert(MMA_SU * MMA_SV <= MMA_PL && MMA_PL % 32 == 16, "stage plane layout");
+constexpr int MMA_STAGE = 12 * MMA_PL;                                   // floats per warp
+
 template <bool SPLIT>
 __global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid g, int side, float memory,
                                                                      const uint32_t *Wp, const float *E,
                                                                      const float *H, float *pred)
 {
-    extern __shared__ __align__(16) uint32_t smem[];
-    uint32_t *w = smem;                                                   // LBC_PACK_WORDS
-    float *xs_all = reinterpret_cast<float *>(smem + LBC_PACK_WORDS);     // [warps][16][XS]
-    float *r_all = xs_all + MMA_WARPS * 16 * XS;                          // [warps][16] RMS of each row
+    extern __shared__ __align__(16) float smem_f[];
     const LFace &f = g.face[blockIdx.y];
     if (side >= 0 && f.side != side) return;                             // block-uniform
-    {
-        const uint4 *src = reinterpret_cast<const uint4 *>(Wp + (uint64_t)(f.axis * 2 + f.side) * LBC_PACK_WORDS);
-        uint4 *dst = reinterpret_cast<uint4 *>(w);
-        for (int i = threadIdx.x; i < LBC_PACK_WORDS / 4; i += blockDim.x) dst[i] = src[i];
-    }
-    __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gq = lane >> 2, tq = lane & 3;
-    float *xs = xs_all + warp * 16 * XS;
-    float *rr = r_all + warp * 16;
+    float *st = smem_f + warp * (MMA_STAGE + 16 * XS + 16);
+    float *xs = st + MMA_STAGE;                                           // [16][XS] network inputs
+    float *rr = xs + 16 * XS;                                             // [16] RMS of each row
+    // packed weights of the face (read through L1: every warp of the face reads the same 24 KB)
+    const uint32_t *w = Wp + (uint64_t)(f.axis * 2 + f.side) * LBC_PACK_WORDS;
     const float *wb = reinterpret_cast<const float *>(w);
     const uint2 *w1 = reinterpret_cast<const uint2 *>(w + PK_W1);
     const uint2 *w2 = reinterpret_cast<const uint2 *>(w + PK_W2);
     const uint2 *w3 = reinterpret_cast<const uint2 *>(w + PK_W3);
-    for (int tile = 0; tile < MMA_TILES; ++tile) {
-        const uint32_t cbase = blockIdx.x * MMA_COLS + (tile * MMA_WARPS + warp) * 16;
-        if (cbase >= f.ncol) break;                                       // warp-uniform
+
+    const uint32_t ntv = (f.nv + 15u) / 16u, ntu = (f.nu + MMA_TU - 1u) / MMA_TU;
+    const uint32_t job = blockIdx.x * MMA_WARPS + warp;
+    if (job >= ntu * ntv) return;                                         // warp-uniform; no block barrier below
+    const uint32_t tu = job / ntv, tv = job % ntv;
+    const uint32_t cu0 = tu * MMA_TU, cv0 = tv * 16u;                     // first column of the tile (face-local)
+    {
+        // stage: cells (u0 + cu0 - 1 + su, v0 + cv0 - 1 + sv), clamped to the grid like cell_of.
+        // Per (component, su) row of the stage a lane loads the pairs (sv, d) number lane and
+        // lane + 32 of 36, ordered (sv, d) on z faces (the depth pair is contiguous in memory)
+        // and (d, sv) on x and y faces (v = z is contiguous).
+        const int a = f.axis, ua = a == 0 ? 1 : 0, va = a == 2 ? 1 : 2;
+        const uint64_t syz = (uint64_t)g.s[1] * g.s[2];
+        const uint64_t sd = a == 0 ? syz : a == 1 ? (uint64_t)g.s[2] : 1u;     // strides of the depth,
+        const uint64_t sua = ua == 0 ? syz : (uint64_t)g.s[2];                 // u and v axes
+        const uint64_t sva = va == 1 ? (uint64_t)g.s[2] : 1u;
+        uint64_t off[2];
+        int soff[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int e = lane + 32 * h < 2 * MMA_SV ? lane + 32 * h : 0;
+            const int d = a == 2 ? (e & 1) : e / MMA_SV;
+            const int sv = a == 2 ? (e >> 1) : e % MMA_SV;
+            const uint32_t cd = f.side ? g.s[a] - 1u - (uint32_t)d : (uint32_t)d;
+            const uint32_t cv = clampu((int)(f.v0 + cv0) - 1 + sv, g.s[va]);
+            off[h] = cd * sd + cv * sva;
+            soff[h] = d * MMA_PL + sv;
+        }
+        const bool second = lane + 32 < 2 * MMA_SV;
+#pragma unroll 1
+        for (int su = 0; su < MMA_SU; ++su) {
+            const uint64_t ou = clampu((int)(f.u0 + cu0) - 1 + su, g.s[ua]) * sua;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const float *src = q < 3 ? E + q * g.N : H + (q - 3) * g.N;
+                float *dst = st + q * 2 * MMA_PL + su * MMA_SV;
+                dst[soff[0]] = src[ou + off[0]];
+                if (second) dst[soff[1]] = src[ou + off[1]];
+            }
+        }
+    }
+    __syncwarp();
+    for (int tr = 0; tr < MMA_TU; ++tr) {
+        const uint32_t cu = cu0 + (uint32_t)tr;
+        if (cu >= f.nu) break;                                            // warp-uniform
         // gather: lane pair (row = lane / 2) reads depth (lane & 1) of its column's stencil
         {
             const int row = lane >> 1, d = lane & 1;
-            const uint32_t c = cbase + row;
-            const uint32_t cc = c < f.ncol ? c : cbase;
-            const uint32_t u = f.u0 + cc / f.nv, v = f.v0 + cc % f.nv;
+            const uint32_t cv = cv0 + (uint32_t)row;
+            const uint32_t u = f.u0 + cu, v = f.v0 + cv;
             // columns outside the window read nothing: r = 0, no network term
-            const bool ok = c < f.ncol && in_window(g, blockIdx.y, u, v);
+            const bool ok = cv < f.nv && in_window(g, blockIdx.y, u, v);
             float x[54];
             float ss = 0.f;
 #pragma unroll
             for (int du = -1; du <= 1; ++du)
 #pragma unroll
                 for (int dv = -1; dv <= 1; ++dv) {
-                    const uint64_t i = cell_of(g, f, u, v, d, du, dv);
                     const int k0 = ((du + 1) * 3 + (dv + 1)) * 6;
+                    const float *sp = st + d * MMA_PL + (tr + 1 + du) * MMA_SV + (row + 1 + dv);
 #pragma unroll
                     for (int q = 0; q < 6; ++q) {
-                        const float xv = ok ? (q < 3 ? E[q * g.N + i] : H[(q - 3) * g.N + i]) : 0.f;
+                        const float xv = ok ? sp[q * 2 * MMA_PL] : 0.f;
                         x[k0 + q] = xv;
                         ss += xv * xv;
                     }
@@ -570,7 +631,7 @@ __global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid 
         float acc[8][4];
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt) {
-            const float b0 = wb[PK_B1 + 8 * nt + 2 * tq], b1 = wb[PK_B1 + 8 * nt + 2 * tq + 1];
+            const float b0 = __ldg(wb + PK_B1 + 8 * nt + 2 * tq), b1 = __ldg(wb + PK_B1 + 8 * nt + 2 * tq + 1);
             acc[nt][0] = b0; acc[nt][1] = b1; acc[nt][2] = b0; acc[nt][3] = b1;
         }
 #pragma unroll
@@ -593,7 +654,7 @@ __global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid 
             }
 #pragma unroll
             for (int nt = 0; nt < 8; ++nt) {
-                const uint2 b = w1[(ks * 8 + nt) * 32 + lane];
+                const uint2 b = __ldg(w1 + (ks * 8 + nt) * 32 + lane);
                 mma_bf16(acc[nt], ah, b.x, b.y);
                 if (SPLIT) mma_bf16(acc[nt], al, b.x, b.y);
             }
@@ -603,14 +664,14 @@ __global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid 
         // layer 2: [16 x 64] x [64 x 64]
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt) {
-            const float b0 = wb[PK_B2 + 8 * nt + 2 * tq], b1 = wb[PK_B2 + 8 * nt + 2 * tq + 1];
+            const float b0 = __ldg(wb + PK_B2 + 8 * nt + 2 * tq), b1 = __ldg(wb + PK_B2 + 8 * nt + 2 * tq + 1);
             acc[nt][0] = b0; acc[nt][1] = b1; acc[nt][2] = b0; acc[nt][3] = b1;
         }
 #pragma unroll
         for (int ks = 0; ks < 4; ++ks)
 #pragma unroll
             for (int nt = 0; nt < 8; ++nt) {
-                const uint2 b = w2[(ks * 8 + nt) * 32 + lane];
+                const uint2 b = __ldg(w2 + (ks * 8 + nt) * 32 + lane);
                 mma_bf16(acc[nt], ah2[ks], b.x, b.y);
                 if (SPLIT) mma_bf16(acc[nt], al2[ks], b.x, b.y);
             }
@@ -618,12 +679,12 @@ __global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid 
         // layer 3: [16 x 64] x [64 x 8]
         float y[4];
         {
-            const float b0 = wb[PK_B3 + 2 * tq], b1 = wb[PK_B3 + 2 * tq + 1];
+            const float b0 = __ldg(wb + PK_B3 + 2 * tq), b1 = __ldg(wb + PK_B3 + 2 * tq + 1);
             y[0] = b0; y[1] = b1; y[2] = b0; y[3] = b1;
         }
 #pragma unroll
         for (int ks = 0; ks < 4; ++ks) {
-            const uint2 b = w3[ks * 32 + lane];
+            const uint2 b = __ldg(w3 + ks * 32 + lane);
             mma_bf16(y, ah2[ks], b.x, b.y);
             if (SPLIT) mma_bf16(y, al2[ks], b.x, b.y);
         }
@@ -632,8 +693,9 @@ __global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid 
 #pragma unroll
             for (int hr = 0; hr < 2; ++hr) {
                 const int row = gq + 8 * hr;
-                const uint32_t c = cbase + row;
-                if (c < f.ncol) {
+                const uint32_t cv = cv0 + (uint32_t)row;
+                if (cv < f.nv) {
+                    const uint32_t c = cu * f.nv + cv;
                     const float r = rr[row];
                     float *out = pred + (uint64_t)(f.col0 + c) * LBC_OUT + 2 * tq;
                     out[0] = (r > 0.f ? y[2 * hr] * r : 0.f) + memory * out[0];
@@ -645,7 +707,7 @@ __global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid 
     }
 }
 
-constexpr size_t MMA_SMEM = (size_t)LBC_PACK_WORDS * 4 + (size_t)MMA_WARPS * 16 * (XS + 1) * 4;
+constexpr size_t MMA_SMEM = (size_t)MMA_WARPS * (MMA_STAGE + 16 * XS + 16) * 4;
 
 // Levi-Civita sign of distinct (q, a, p): +1 for the cyclic orders of (0, 1, 2)
 __device__ __forceinline__ float lc(int q, int a) { return ((a - q + 3) % 3) == 1 ? 1.f : -1.f; }
@@ -886,7 +948,12 @@ cudaError_t launch_lbc_predict(const LGrid &g, int side, int precision, float me
     const cudaError_t e = split ? smem_opt_in((const void *)k_lbc_predict_mma<true>, SMEM_MMA_SPLIT, MMA_SMEM)
                                 : smem_opt_in((const void *)k_lbc_predict_mma<false>, SMEM_MMA, MMA_SMEM);
     if (e != cudaSuccess) return e;
-    const dim3 gi((maxc + MMA_COLS - 1) / MMA_COLS, (unsigned)g.nface, 1);
+    uint32_t maxj = 0;
+    for (int f = 0; f < g.nface; ++f) {
+        const uint32_t nj = ((g.face[f].nu + MMA_TU - 1) / MMA_TU) * ((g.face[f].nv + 15) / 16);
+        maxj = nj > maxj ? nj : maxj;
+    }
+    const dim3 gi((maxj + MMA_WARPS - 1) / MMA_WARPS, (unsigned)g.nface, 1);
     if (split)
         k_lbc_predict_mma<true><<<gi, MMA_WARPS * 32, MMA_SMEM, st>>>(g, side, memory, (const uint32_t *)W, E, H, pred);
     else
