@@ -446,13 +446,38 @@ __device__ __forceinline__ void split_bf16(float x0, float x1, uint32_t &hi, uin
 // with the exponential and reciprocal on the special-function unit; well inside the bfloat16
 // (and split-bfloat16) precision of the layer inputs it feeds. Training and the float32 checker
 // use erff.
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// PTX: the reciprocal and 2^x by rcp.approx / ex2.approx and the last step as one fma;
+// otherwise the __fdividef / __expf intrinsics. Same approximation either way; each form
+// measured faster in one of the two kernels (bf16x2: PTX, bf16: intrinsics).
+template <bool PTX>
 __device__ __forceinline__ float gelu_mma(float x)
 {
-    const float z = x * 0.70710678118654752f;
+    const float z = x * 0.70710678118654752f;                 // x / sqrt(2)
     const float az = fabsf(z);
-    const float t = __fdividef(1.0f, fmaf(0.3275911f, az, 1.0f));
+    const float den = fmaf(0.3275911f, az, 1.0f);
+    const float t = PTX ? rcp_approx(den) : __fdividef(1.0f, den);
     const float poly = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f),
                                         -0.284496736f), 0.254829592f);
+    if (PTX) {
+        // exp(-z^2) = 2^(-z^2 log2(e))
+        const float e = copysignf(fmaf(-poly, ex2_approx((az * az) * -1.4426950408889634f), 1.0f), z);
+        const float h = 0.5f * x;
+        return fmaf(h, e, h);                                 // x (1 + erf(z)) / 2
+    }
     const float e = copysignf(1.0f - poly * __expf(-az * az), z);
     return 0.5f * x * (1.0f + e);
 }
@@ -504,7 +529,8 @@ __device__ __forceinline__ void act_to_a(const float acc[8][4], uint32_t ah[4][4
 #pragma unroll
         for (int half = 0; half < 2; ++half) {
             const float *c = acc[2 * ks + half];
-            const float g0 = gelu_mma(c[0]), g1 = gelu_mma(c[1]), g2 = gelu_mma(c[2]), g3 = gelu_mma(c[3]);
+            const float g0 = gelu_mma<SPLIT>(c[0]), g1 = gelu_mma<SPLIT>(c[1]);
+            const float g2 = gelu_mma<SPLIT>(c[2]), g3 = gelu_mma<SPLIT>(c[3]);
             if (SPLIT) {
                 split_bf16(g0, g1, ah[ks][2 * half], al[ks][2 * half]);
                 split_bf16(g2, g3, ah[ks][2 * half + 1], al[ks][2 * half + 1]);
@@ -616,12 +642,12 @@ __global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid 
             ss += __shfl_xor_sync(0xffffffffu, ss, 1);
             const float r = sqrtf(ss * (1.0f / LBC_IN));
             const float inv = r > 0.f ? 1.0f / r : 0.f;
-            float *xr = xs + row * XS + d * 54;
+            float2 *xr = reinterpret_cast<float2 *>(xs + row * XS + d * 54);   // 8-byte aligned
 #pragma unroll
-            for (int k = 0; k < 54; ++k) xr[k] = x[k] * inv;
+            for (int k = 0; k < 27; ++k) xr[k] = make_float2(x[2 * k] * inv, x[2 * k + 1] * inv);
             if (d == 1) {
-#pragma unroll
-                for (int k = 108 - 54; k < 112 - 54; ++k) xr[k] = 0.f;   // K padding 108..111
+                xr[27] = make_float2(0.f, 0.f);                           // K padding 108..111
+                xr[28] = make_float2(0.f, 0.f);
             } else {
                 rr[row] = r;
             }
