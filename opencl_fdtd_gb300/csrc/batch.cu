@@ -169,7 +169,10 @@ struct BELoad {
     float xu, xv, yu, yv, zu, zv;
 };
 
-template <int ST>
+// PF: the next plane's loads are issued before the current plane's arithmetic (latency hidden
+// by instruction-level parallelism, twice the registers for loaded values); without, latency
+// is hidden by more resident warps.
+template <int ST, bool PF = true>
 __device__ void batch_e_tile(const BVar &v, int4 tl, int64_t step, int64_t rows)
 {
     using SS = Store<ST>;
@@ -237,14 +240,15 @@ __device__ void batch_e_tile(const BVar &v, int4 tl, int64_t step, int64_t rows)
         const int32_t wm = SS::scaled ? hexp[texp_index(v, xm, jt)] : 0;
         hy_m = dv<ST>(ldr(Hy + im), xe(wm, 1));
         hz_m = dv<ST>(ldr(Hz + im), xe(wm, 2));
-        cur = load(xa);
+        if (PF) cur = load(xa);
     }
     for (uint32_t x = xa; x < xb; ++x) {
         const uint32_t i = x * syz + j;
         BELoad<T> nxt;
         float nx = 0.f, ny = 0.f, nz = 0.f, hy = 0.f, hz = 0.f;
         if (act) {
-            if (x + 1u < xb) nxt = load(x + 1u);
+            if (!PF) cur = load(x);
+            else if (x + 1u < xb) nxt = load(x + 1u);
             const float hx = dv<ST>(cur.hx, xe(cur.gh, 0));
             hy = dv<ST>(cur.hy, xe(cur.gh, 1));
             hz = dv<ST>(cur.hz, xe(cur.gh, 2));
@@ -321,7 +325,7 @@ __device__ void batch_e_tile(const BVar &v, int4 tl, int64_t step, int64_t rows)
             }
             hy_m = hy;
             hz_m = hz;
-            cur = nxt;
+            if (PF) cur = nxt;
         }
     }
 }
@@ -334,7 +338,7 @@ struct BHLoad {
     float xu, xv, yu, yv, zu, zv;
 };
 
-template <int ST>
+template <int ST, bool PF = true>
 __device__ void batch_h_tile(const BVar &v, int4 tl)
 {
     using SS = Store<ST>;
@@ -402,14 +406,15 @@ __device__ void batch_h_tile(const BVar &v, int4 tl)
         ex = dv<ST>(ldr(Ex + i), xe(wa, 0));
         ey = dv<ST>(ldr(Ey + i), xe(wa, 1));
         ez = dv<ST>(ldr(Ez + i), xe(wa, 2));
-        cur = load(xa);
+        if (PF) cur = load(xa);
     }
     for (uint32_t x = xa; x < xb; ++x) {
         const uint32_t i = x * syz + j;
         BHLoad<T> nxt;
         float nx = 0.f, ny = 0.f, nz = 0.f, ex1 = 0.f, ey1 = 0.f, ez1 = 0.f;
         if (act) {
-            if (x + 1u < xb) nxt = load(x + 1u);
+            if (!PF) cur = load(x);
+            else if (x + 1u < xb) nxt = load(x + 1u);
             ex1 = dv<ST>(cur.ex1, xe(cur.ge, 0));
             ey1 = dv<ST>(cur.ey1, xe(cur.ge, 1));
             ez1 = dv<ST>(cur.ez1, xe(cur.ge, 2));
@@ -465,23 +470,23 @@ __device__ void batch_h_tile(const BVar &v, int4 tl)
             ex = ex1;
             ey = ey1;
             ez = ez1;
-            cur = nxt;
+            if (PF) cur = nxt;
         }
     }
 }
 
-template <int ST>
+template <int ST, bool PF>
 __device__ __forceinline__ void batch_e_item(const BatchK &k, uint32_t ti, int64_t step)
 {
     const int4 tl = k.tiles[ti];
-    batch_e_tile<ST>(k.vars[tl.x], tl, step, k.rows);
+    batch_e_tile<ST, PF>(k.vars[tl.x], tl, step, k.rows);
 }
 
-template <int ST>
+template <int ST, bool PF>
 __device__ __forceinline__ void batch_h_item(const BatchK &k, uint32_t ti)
 {
     const int4 tl = k.tiles[ti];
-    batch_h_tile<ST>(k.vars[tl.x], tl);
+    batch_h_tile<ST, PF>(k.vars[tl.x], tl);
 }
 
 // next tile of the half-step whose counter is `ctr` (>= ntiles: none left)
@@ -493,8 +498,13 @@ __device__ __forceinline__ uint32_t next_tile(uint32_t *ctr, uint32_t *slot)
     return *slot;
 }
 
+// Persistent form: without the register prefetch (PF false) the E and H tile bodies together
+// fit BATCH_PERSIST_BLOCKS resident blocks per SM (64 registers), whose warps hide the load
+// latency; with it they need 128 registers and two blocks per SM, 1.3x slower.
+constexpr int BATCH_PERSIST_BLOCKS = 4;
+
 template <int ST>
-__global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(const BatchK k)
+__global__ void __launch_bounds__(BATCH_THREADS, BATCH_PERSIST_BLOCKS) k_batch(const BatchK k)
 {
     __shared__ uint32_t item;
     cg::grid_group grid = cg::this_grid();
@@ -504,11 +514,11 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(const BatchK k)
         // half-step 2t uses counter 0, 2t + 1 counter 1; a counter is cleared right after the
         // grid barrier that ends its half-step, two barriers before its next use
         for (uint32_t ti = next_tile(&k.work[0], &item); ti < k.ntiles; ti = next_tile(&k.work[0], &item))
-            batch_e_item<ST>(k, ti, step);
+            batch_e_item<ST, false>(k, ti, step);
         grid.sync();
         if (blockIdx.x == 0 && threadIdx.x == 0) k.work[0] = 0u;
         for (uint32_t ti = next_tile(&k.work[1], &item); ti < k.ntiles; ti = next_tile(&k.work[1], &item))
-            batch_h_item<ST>(k, ti);
+            batch_h_item<ST, false>(k, ti);
         grid.sync();
         if (blockIdx.x == 0 && threadIdx.x == 0) k.work[1] = 0u;
     }
@@ -516,9 +526,9 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(const BatchK k)
     if (blockIdx.x == 0 && threadIdx.x == 0) *k.step = step0 + k.nsteps;
 }
 
-// One tile per block, all variants' tiles in one launch per half-step (the hardware block
-// scheduler keeps ~3 blocks per SM busy and overlaps one block's first loads with another's
-// arithmetic, which the persistent loop cannot). The H launch advances the step counter.
+// One tile per block, all variants' tiles in one launch per half-step: three blocks per SM,
+// each warp with two planes of loads in flight (the register prefetch), about 1.5x the loads
+// in flight of the persistent form. The H launch advances the step counter.
 template <int ST>
 __global__ void __launch_bounds__(BATCH_THREADS, 3) k_batch_e(const BatchK k)
 {
