@@ -197,7 +197,8 @@ __device__ __forceinline__ void hs_math(const HSK<R> &k, uint32_t x, uint32_t y,
 // barrier per plane waits for no extra work. The products go to shared memory slots that
 // alternate by plane, which is what lets one barrier per plane suffice.
 // PF: issue the next plane's loads before the current plane's arithmetic (one block per SM
-// with room for both sets of registers) or not (two blocks per SM, fewer registers each).
+// with room for both sets of registers); otherwise (two blocks per SM) they are issued after
+// the products are stored, so they are in flight during the barrier and the S assembly.
 template <typename R, int DX, bool MU, bool PF>
 __global__ void __launch_bounds__(HS_THREADS, PF ? 1 : 2) k_bulk_hs(const HSK<R> k)
 {
@@ -238,14 +239,13 @@ __global__ void __launch_bounds__(HS_THREADS, PF ? 1 : 2) k_bulk_hs(const HSK<R>
     }
     HSLoad<R> cur;
     uint32_t i = xa * syz + j;
-    if (PF && act) hs_load<R, MU>(k, xa, i, dpy, dpz, hs_face<R>(k.ax[0], sx, xa), fy, fz, y, z, cur);
+    if (act) hs_load<R, MU>(k, xa, i, dpy, dpz, hs_face<R>(k.ax[0], sx, xa), fy, fz, y, z, cur);
     for (uint32_t x = xa; x < xb; ++x, i += syz) {
         const HSF fx = hs_face<R>(k.ax[0], sx, x);
         const int slot = (int)(x & 1u);
         HSLoad<R> nxt;
         if (act) {
-            if (!PF) hs_load<R, MU>(k, x, i, dpy, dpz, fx, fy, fz, y, z, cur);
-            else if (x + 1u < xb) hs_load<R, MU>(k, x + 1u, i + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, nxt);
+            if (PF && x + 1u < xb) hs_load<R, MU>(k, x + 1u, i + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, nxt);
             R os[6];
             hs_math<R, DX, MU>(k, x, y, z, i, fx, fy, fz, cur, own, os);
 #pragma unroll
@@ -254,6 +254,9 @@ __global__ void __launch_bounds__(HS_THREADS, PF ? 1 : 2) k_bulk_hs(const HSK<R>
 #pragma unroll
                 for (int c = 0; c < 6; ++c) k.oS[(uint64_t)c * N + i] = os[c];
             }
+            // the next plane's loads fly during the barrier and the S assembly
+            if (!PF && x + 1u < xb)
+                hs_load<R, MU>(k, x + 1u, i + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, cur);
         }
         __syncthreads();
         if (own) {
