@@ -637,8 +637,13 @@ def main():
             "clocks": clock, "e2e": e2e, "gpu_launches": hp["gpu_launches"],
             "cpu_baseline": cpu,
             "dropin_roofline": out_paths["dropin"]["roofline"] if "dropin" in out_paths else None,
+            # roofline_frac: the path's own kernel (dropin: its dominant kernel per launch);
+            # step_roofline_frac: the whole step against the step's algorithmic bytes, the same
+            # basis for every path (the per-call loop moves more than those bytes: it writes
+            # and re-reads the six Poynting products)
             "paths": {k: {"value": round(v["value"], 2), "ms_per_step": round(v["ms_per_step"], 5),
-                          "roofline_frac": v["roofline"]["frac"], "kernel": v["roofline"]["kernel"]}
+                          "roofline_frac": v["roofline"]["frac"], "kernel": v["roofline"]["kernel"],
+                          "step_roofline_frac": round(step_bytes / (v["ms_per_step"] * 1e-3) / 1e9 / peak, 4)}
                       for k, v in out_paths.items()},
         }
         out.update(extras)
