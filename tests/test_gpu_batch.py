@@ -1,7 +1,8 @@
 """Batched stepping of several variants in one persistent launch (BatchSimulation): float32
 storage is bit-identical to stepping each variant with Simulation.run, for every tile shape,
 through CUDA-graph replays and monitor series; 16-bit storage with per-tile exponents stays
-close to the float32 result and its encode/decode round trip is within the format's rounding."""
+close to the float32 result, its encode/decode round trip is within the format's rounding,
+and on the seeded cavity variants its error against float64 stays within stated bounds."""
 import copy
 import math
 
@@ -237,3 +238,56 @@ def test_batch_f32_variant_equals_oracle(schedule):
         for k in ("E", "H"):
             x = getattr(got[v], k).detach().cpu().numpy().reshape(-1)
             assert numpy.array_equal(x, getattr(c, k).reshape(-1)), (v, k)
+
+
+def _cavity_errors(storages, n_variants=4, steps=400):
+    """Relative L2 of E against a float64 run of each of the first n_variants seeded c4 cavity
+    variants after `steps` steps of the centre dipole pulse, per storage (the setting of the
+    benchmark's batched section)."""
+    from opencl_fdtd_gb300 import Simulation, workloads
+    from opencl_fdtd_gb300.batch import BatchSimulation
+    variants = workloads.c4(n=n_variants, steps=steps)
+    wave = numpy.array([variants[0]["wave"](t) for t in range(steps)], dtype=numpy.float64)
+    refs = []
+    for var in variants:
+        kw64, ind = workloads.c4_kwargs(var, float_type=numpy.float64)
+        s64 = Simulation(**kw64)
+        s64.run(steps, point_sources=[(ind, wave)], path="plain")
+        refs.append(s64.E.clone())
+        del s64
+    out = {}
+    for storage in storages:
+        sims, idx = [], []
+        for var in variants:
+            kw, ind = workloads.c4_kwargs(var)
+            sims.append(Simulation(**kw))
+            idx.append(ind)
+        b = BatchSimulation(sims, storage=storage, sources=[[(i, wave)] for i in idx], steps=steps)
+        b.run(steps)
+        b.sync()
+        torch.cuda.synchronize()
+        errs = []
+        for s, ref in zip(sims, refs):
+            fin = torch.isfinite(ref)
+            errs.append(float(torch.linalg.norm((s.E.double() - ref)[fin]) / torch.linalg.norm(ref[fin])))
+        out[storage] = errs
+        b.close()
+        del b, sims
+    return out
+
+
+# Bounds of the relative L2 of E against float64 (median, max over the variants) after 400
+# steps on the cavity variants, about twice the measured values (float32 0.8-1.2e-7, bfloat16
+# with or without tile exponents 4.0-6.5e-3, float16 5.4-7.0e-4); the benchmark's batched
+# section reports the same quantity (bfloat16 without exponents: 5.1e-3 / 5.7e-3 on 16 of
+# the variants). bfloat16 with and without exponents differ in the bits here: the pulse's
+# leading edge holds float32-subnormal values, where a tile exponent changes the rounding.
+CAVITY_BOUNDS = {"f32": (3e-7, 3e-7), "bf16": (1e-2, 1.3e-2), "bf16u": (1e-2, 1.3e-2), "fp16": (1.5e-3, 1.5e-3)}
+
+
+def test_batch_16bit_error_vs_float64_on_cavity_variants():
+    errs = _cavity_errors(tuple(CAVITY_BOUNDS))
+    print({k: ["%.3g" % e for e in v] for k, v in errs.items()})
+    for storage, (med, mx) in CAVITY_BOUNDS.items():
+        e = numpy.array(errs[storage])
+        assert numpy.median(e) <= med and e.max() <= mx, (storage, e)
