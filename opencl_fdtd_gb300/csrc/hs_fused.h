@@ -6,8 +6,10 @@
 namespace fdtd {
 
 // threads of an H+S block: whole z rows, the block's own rows plus one halo row,
-// rows = HS_THREADS / sz - 1
-constexpr int HS_THREADS = 512;
+// rows = HS_THREADS / sz - 1 (z rows of at most HS_THREADS / 2 cells). Two blocks per SM of
+// 448 threads leave 72 registers a thread; 512 threads (64 registers, more spilled) ran 5%
+// slower on 73-cell rows, 384 threads (4 own rows per halo row) 1% slower.
+constexpr int HS_THREADS = 448;
 
 // H-side CPML faces of one axis: tables [n/p][p0,p1,p2], old (A) and new (B) psi [n/p][u/v].
 // Tp = 0 when the 'p' face never applies.

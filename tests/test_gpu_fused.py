@@ -187,7 +187,8 @@ def test_slab_schedule_bloch_mu():
             assert torch.equal(getattr(a, k), getattr(b, k)), (slab, k)
 
 
-HS_SHAPES = [((16, 14, 12), 3), ((10, 9, 200), 3), ((6, 5, 511), 2), ((9, 11, 100), 4), ((7, 6, 300), 1)]
+HS_SHAPES = [((16, 14, 12), 3), ((10, 9, 200), 3), ((6, 5, 511), 2), ((9, 11, 100), 4), ((7, 6, 300), 1),
+             ((5, 6, 224), 2), ((6, 7, 73), 2)]
 
 
 @pytest.mark.parametrize("shape,T", HS_SHAPES)
@@ -195,7 +196,8 @@ HS_SHAPES = [((16, 14, 12), 3), ((10, 9, 200), 3), ((6, 5, 511), 2), ((9, 11, 10
 @pytest.mark.parametrize("nsteps", [5, 8])
 def test_hs_path_equals_per_call_loop(shape, T, xchunk, nsteps):
     """run(path='hs'): H and S in one launch, with blocks of whole z rows so that several
-    blocks (and, for sz > 256, one-row blocks) recompute their first row's y-1 products."""
+    blocks (and, for sz > 149, one-row blocks) recompute their first row's y-1 products; rows
+    longer than 224 cells take the per-update kernels."""
     rng = numpy.random.default_rng(sum(shape) + T)
     eps = [rng.uniform(1, 4, shape).astype(numpy.float32) for _ in range(3)]
     eps[1][1:3, 2:4, 5:9] = numpy.inf
