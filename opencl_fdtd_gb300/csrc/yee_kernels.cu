@@ -240,10 +240,13 @@ struct ELoad {
     R xu, xv, yu, yv, zu, zv;     // psi of the faces the cell is in
 };
 
+// block shape of the bulk E kernel: EBLOCK threads, at least EMINB blocks per SM
+constexpr int EBLOCK = 256, EMINB = 3;
+
 template <typename R, int DX, bool BLOCH>
-__global__ void __launch_bounds__(BLOCK, 3) k_bulk_e(const YeeK<R> k)
+__global__ void __launch_bounds__(EBLOCK, EMINB) k_bulk_e(const YeeK<R> k)
 {
-    const uint32_t j = blockIdx.x * BLOCK + threadIdx.x;
+    const uint32_t j = blockIdx.x * EBLOCK + threadIdx.x;
     if (j >= k.syz) return;
     const uint32_t sx = k.sx, sy = k.sy, sz = k.sz, syz = k.syz;
     const uint32_t y = k.dsz.div(j);
@@ -609,9 +612,9 @@ __global__ void k_point_sources(const PointK<R> k)
 }
 
 // ---- launchers ------------------------------------------------------------------------------
-static inline dim3 bulk_grid(uint32_t syz, uint32_t nx, int xchunk)
+static inline dim3 bulk_grid(uint32_t syz, uint32_t nx, int xchunk, uint32_t block = BLOCK)
 {
-    return dim3((syz + BLOCK - 1) / BLOCK, (nx + (uint32_t)xchunk - 1) / (uint32_t)xchunk, 1);
+    return dim3((syz + block - 1) / block, (nx + (uint32_t)xchunk - 1) / (uint32_t)xchunk, 1);
 }
 
 static inline dim3 plane_grid(uint32_t syz, uint32_t nx)
@@ -627,15 +630,15 @@ cudaError_t launch_yee_e(const YeeK<R> &k, cudaStream_t st)
         k_generic_e<R><<<plane_grid(k.syz, k.xend - k.xbeg), BLOCK, 0, st>>>(k);
         return cudaGetLastError();
     }
-    const dim3 g = bulk_grid(k.syz, k.xend - k.xbeg, k.xchunk);
+    const dim3 g = bulk_grid(k.syz, k.xend - k.xbeg, k.xchunk, EBLOCK);
     if (k.bloch_mask) {
-        if (k.dxmode == 0) k_bulk_e<R, 0, true><<<g, BLOCK, 0, st>>>(k);
-        else if (k.dxmode == 1) k_bulk_e<R, 1, true><<<g, BLOCK, 0, st>>>(k);
-        else k_bulk_e<R, 2, true><<<g, BLOCK, 0, st>>>(k);
+        if (k.dxmode == 0) k_bulk_e<R, 0, true><<<g, EBLOCK, 0, st>>>(k);
+        else if (k.dxmode == 1) k_bulk_e<R, 1, true><<<g, EBLOCK, 0, st>>>(k);
+        else k_bulk_e<R, 2, true><<<g, EBLOCK, 0, st>>>(k);
     } else {
-        if (k.dxmode == 0) k_bulk_e<R, 0, false><<<g, BLOCK, 0, st>>>(k);
-        else if (k.dxmode == 1) k_bulk_e<R, 1, false><<<g, BLOCK, 0, st>>>(k);
-        else k_bulk_e<R, 2, false><<<g, BLOCK, 0, st>>>(k);
+        if (k.dxmode == 0) k_bulk_e<R, 0, false><<<g, EBLOCK, 0, st>>>(k);
+        else if (k.dxmode == 1) k_bulk_e<R, 1, false><<<g, EBLOCK, 0, st>>>(k);
+        else k_bulk_e<R, 2, false><<<g, EBLOCK, 0, st>>>(k);
     }
     return cudaGetLastError();
 }
