@@ -97,7 +97,8 @@ typedef struct FdtdBuffers {
     void *ce, *cm;
     /* Optional second copies for fdtd_run (same sizes as E, H, psi_e, psi_h). With H2 and every
      * psi_h2 set (E2 NULL), steps run update_E in place and H and S in one launch that reads
-     * one copy of H and writes the other. With E2, H2 and every psi_e2 / psi_h2 set, each step
+     * one copy of H and writes the other (z rows of at most 224 cells; longer rows, Bloch
+     * boundaries or overlapping CPML faces use the per-update kernels). With E2, H2 and every psi_e2 / psi_h2 set, each step
      * is one launch of the one-pass kernel, which reads one copy of everything and writes the
      * other. At the end the result is always back in E, H, psi_e, psi_h. When NULL, fdtd_run
      * uses the per-update kernels. Results are identical either way. */
