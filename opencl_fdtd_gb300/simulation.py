@@ -497,14 +497,17 @@ class Simulation:
             idx = numpy.array([int(i) for i, _ in point_sources], dtype=numpy.int64)
             if (idx < 0).any() or (idx >= 3 * self.N).any():
                 raise IndexError("point source index out of range")
-            vals = numpy.zeros((nsteps, n), dtype=self._np_dtype)
+            # staged in pinned host memory and copied without blocking the host: the caching
+            # host allocator keeps the staging block until the copy on `stream` has run
+            pinned = torch.empty((max(nsteps, 1), n), dtype=self.E.dtype, pin_memory=True)
+            vals = pinned.numpy()
             for k, (_, v) in enumerate(point_sources):
                 v = numpy.asarray(v, dtype=numpy.float64).ravel()
                 if v.size < nsteps:
                     raise ValueError("point source {} has {} values for {} steps".format(k, v.size, nsteps))
-                vals[:, k] = v[:nsteps]
+                vals[:nsteps, k] = v[:nsteps]
             with torch.cuda.stream(stream):
-                val_t = torch.from_numpy(vals).to(self.device, non_blocking=False)
+                val_t = pinned.to(self.device, non_blocking=True)
             idx_host = (ctypes.c_int64 * n)(*idx.tolist())
             keep = [val_t]
             src = _lib.FdtdPointSources(n, 0, ctypes.addressof(idx_host), val_t.data_ptr())
