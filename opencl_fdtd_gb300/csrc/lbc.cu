@@ -363,50 +363,120 @@ __global__ void __launch_bounds__(T_APPLY) k_lbc_predict32(const LGrid g, int si
     for (int o = 0; o < LBC_OUT; ++o) out[o] = y[o] * r + memory * out[o];
 }
 
-// an exactly linear layer (LBC_LINEAR): one thread per column, 108 x 6 products, weights
-// [6][IN + 1][OUT] float32 in shared memory
-__global__ void __launch_bounds__(T_APPLY) k_lbc_predict_lin(const LGrid g, int side, float memory, const float *W,
-                                                             const float *E, const float *H, float *pred)
+// ---- stencil tiles staged per warp (the linear and the tensor-core inference) ------------------
+// A warp's job: a tile of MMA_TU x 16 columns of one face (MMA_TU rows along u, 16 columns along
+// v). The cells its stencils read, (MMA_TU + 2) x 18 positions x 2 depths x 6 components, are
+// staged once in shared memory, plane (component q, depth d) by plane with a stride of
+// MMA_PL floats (MMA_PL = 16 mod 32, so the two depths a lane pair reads fall in different
+// banks), before the columns are evaluated 16 at a time. The loads follow the memory order:
+// along z (v) on x and y faces, over the depth pair z = 0, 1 (or s - 1, s - 2) first on z faces.
+constexpr int MMA_TU = 4;
+constexpr int MMA_SU = MMA_TU + 2, MMA_SV = 16 + 2;
+constexpr int MMA_PL = 112;
+static_assert(MMA_SU * MMA_SV <= MMA_PL && MMA_PL % 32 == 16, "stage plane layout");
+constexpr int MMA_STAGE = 12 * MMA_PL;                                   // floats per warp
+
+// Stage the cells of the tile whose first (face-local) column is (cu0, cv0) into st.
+__device__ __forceinline__ void stage_tile(const LGrid &g, const LFace &f, uint32_t cu0, uint32_t cv0,
+                                           const float *E, const float *H, float *st, int lane)
+{
+        // stage: cells (u0 + cu0 - 1 + su, v0 + cv0 - 1 + sv), clamped to the grid like cell_of.
+        // Per (component, su) row of the stage a lane loads the pairs (sv, d) number lane and
+        // lane + 32 of 36, ordered (sv, d) on z faces (the depth pair is contiguous in memory)
+        // and (d, sv) on x and y faces (v = z is contiguous).
+        const int a = f.axis, ua = a == 0 ? 1 : 0, va = a == 2 ? 1 : 2;
+        const uint64_t syz = (uint64_t)g.s[1] * g.s[2];
+        const uint64_t sd = a == 0 ? syz : a == 1 ? (uint64_t)g.s[2] : 1u;     // strides of the depth,
+        const uint64_t sua = ua == 0 ? syz : (uint64_t)g.s[2];                 // u and v axes
+        const uint64_t sva = va == 1 ? (uint64_t)g.s[2] : 1u;
+        uint64_t off[2];
+        int soff[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int e = lane + 32 * h < 2 * MMA_SV ? lane + 32 * h : 0;
+            const int d = a == 2 ? (e & 1) : e / MMA_SV;
+            const int sv = a == 2 ? (e >> 1) : e % MMA_SV;
+            const uint32_t cd = f.side ? g.s[a] - 1u - (uint32_t)d : (uint32_t)d;
+            const uint32_t cv = clampu((int)(f.v0 + cv0) - 1 + sv, g.s[va]);
+            off[h] = cd * sd + cv * sva;
+            soff[h] = d * MMA_PL + sv;
+        }
+        const bool second = lane + 32 < 2 * MMA_SV;
+#pragma unroll 1
+        for (int su = 0; su < MMA_SU; ++su) {
+            const uint64_t ou = clampu((int)(f.u0 + cu0) - 1 + su, g.s[ua]) * sua;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const float *src = q < 3 ? E + q * g.N : H + (q - 3) * g.N;
+                float *dst = st + q * 2 * MMA_PL + su * MMA_SV;
+                dst[soff[0]] = src[ou + off[0]];
+                if (second) dst[soff[1]] = src[ou + off[1]];
+            }
+        }
+}
+
+constexpr int MMA_WARPS = 4;                      // warps of a block of the staged kernels
+
+// an exactly linear layer (LBC_LINEAR), weights [6][IN + 1][OUT] float32 in shared memory: a
+// warp stages a tile of 4 x 16 columns (stage_tile) and each lane forms the 108 x 6 products of
+// two of them (column lane % 16 of the tile's rows lane / 16 and lane / 16 + 2), in the order
+// of the stencil
+__global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_lin(const LGrid g, int side, float memory,
+                                                                    const float *W, const float *E,
+                                                                    const float *H, float *pred)
 {
     __shared__ float w[(LBC_IN + 1) * LBC_OUT];
+    __shared__ float stage[MMA_WARPS][MMA_STAGE];
     const LFace &f = g.face[blockIdx.y];
     if (side >= 0 && f.side != side) return;                 // block-uniform
     const float *Wf = W + (uint64_t)(f.axis * 2 + f.side) * (LBC_IN + 1) * LBC_OUT;
     for (int i = threadIdx.x; i < (LBC_IN + 1) * LBC_OUT; i += blockDim.x) w[i] = Wf[i];
     __syncthreads();
-    const uint32_t c = blockIdx.x * T_APPLY + threadIdx.x;
-    if (c >= f.ncol) return;
-    const uint32_t u = f.u0 + c / f.nv, v = f.v0 + c % f.nv;
-    if (!in_window(g, blockIdx.y, u, v)) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t ntv = (f.nv + 15u) / 16u, ntu = (f.nu + MMA_TU - 1u) / MMA_TU;
+    const uint32_t job = blockIdx.x * MMA_WARPS + warp;
+    if (job >= ntu * ntv) return;                            // warp-uniform; no block barrier below
+    const uint32_t cu0 = (job / ntv) * MMA_TU, cv0 = (job % ntv) * 16u;
+    float *st = stage[warp];
+    stage_tile(g, f, cu0, cv0, E, H, st, lane);
+    __syncwarp();
+    const int jv = lane & 15;
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+        const int tr = (lane >> 4) + 2 * h;
+        const uint32_t cu = cu0 + (uint32_t)tr, cv = cv0 + (uint32_t)jv;
+        if (cu >= f.nu || cv >= f.nv) continue;
+        const uint32_t c = cu * f.nv + cv;
         float *out = pred + (uint64_t)(f.col0 + c) * LBC_OUT;
+        if (!in_window(g, blockIdx.y, f.u0 + cu, f.v0 + cv)) {
 #pragma unroll
-        for (int o = 0; o < LBC_OUT; ++o) out[o] = memory * out[o];
-        return;
-    }
-    float acc[LBC_OUT];
+            for (int o = 0; o < LBC_OUT; ++o) out[o] = memory * out[o];
+            continue;
+        }
+        float acc[LBC_OUT];
 #pragma unroll
-    for (int o = 0; o < LBC_OUT; ++o) acc[o] = 0.f;
-    float ss = 0.f;
+        for (int o = 0; o < LBC_OUT; ++o) acc[o] = 0.f;
+        float ss = 0.f;
 #pragma unroll
-    for (int d = 0; d < 2; ++d)
+        for (int d = 0; d < 2; ++d)
 #pragma unroll
-        for (int du = -1; du <= 1; ++du)
+            for (int du = -1; du <= 1; ++du)
 #pragma unroll
-            for (int dv = -1; dv <= 1; ++dv) {
-                const uint64_t i = cell_of(g, f, u, v, d, du, dv);
-                const int k0 = ((d * 3 + (du + 1)) * 3 + (dv + 1)) * 6;
+                for (int dv = -1; dv <= 1; ++dv) {
+                    const int k0 = ((d * 3 + (du + 1)) * 3 + (dv + 1)) * 6;
+                    const float *sp = st + d * MMA_PL + (tr + 1 + du) * MMA_SV + (jv + 1 + dv);
 #pragma unroll
-                for (int q = 0; q < 6; ++q) {
-                    const float xv = q < 3 ? E[q * g.N + i] : H[(q - 3) * g.N + i];
-                    ss += xv * xv;
+                    for (int q = 0; q < 6; ++q) {
+                        const float xv = sp[q * 2 * MMA_PL];
+                        ss += xv * xv;
 #pragma unroll
-                    for (int o = 0; o < LBC_OUT; ++o) acc[o] += xv * w[(k0 + q) * LBC_OUT + o];
+                        for (int o = 0; o < LBC_OUT; ++o) acc[o] += xv * w[(k0 + q) * LBC_OUT + o];
+                    }
                 }
-            }
-    const float r = sqrtf(ss * (1.0f / LBC_IN));
-    float *out = pred + (uint64_t)(f.col0 + c) * LBC_OUT;
+        const float r = sqrtf(ss * (1.0f / LBC_IN));
 #pragma unroll
-    for (int o = 0; o < LBC_OUT; ++o) out[o] = acc[o] + r * w[LBC_IN * LBC_OUT + o] + memory * out[o];
+        for (int o = 0; o < LBC_OUT; ++o) out[o] = acc[o] + r * w[LBC_IN * LBC_OUT + o] + memory * out[o];
+    }
 }
 
 // ---- bfloat16 tensor-core inference (mma.sync m16n8k16, float32 accumulation) ------------------
@@ -423,7 +493,6 @@ constexpr int PK_B2 = PK_B1 + LBC_HID;            // float [64]
 constexpr int PK_B3 = PK_B2 + LBC_HID;            // float [8]
 static_assert(PK_B3 + 8 == LBC_PACK_WORDS, "packed layout size");
 
-constexpr int MMA_WARPS = 4;
 constexpr int XS = 120;                           // float row stride of a warp's stencil tile
 
 // two floats rounded to bfloat16 in one conversion (lo in the low half)
@@ -541,17 +610,6 @@ __device__ __forceinline__ void act_to_a(const float acc[8][4], uint32_t ah[4][4
         }
 }
 
-// A warp's job: a tile of MMA_TU x 16 columns of one face (MMA_TU rows along u, 16 columns along
-// v). The cells its stencils read, (MMA_TU + 2) x 18 positions x 2 depths x 6 components, are
-// staged once in shared memory, plane (component q, depth d) by plane with a stride of
-// MMA_PL floats (MMA_PL = 16 mod 32, so the two depths a lane pair reads fall in different
-// banks), before the columns are evaluated 16 at a time. The loads follow the memory order:
-// along z (v) on x and y faces, over the depth pair z = 0, 1 (or s - 1, s - 2) first on z faces.
-constexpr int MMA_TU = 4;
-constexpr int MMA_SU = MMA_TU + 2, MMA_SV = 16 + 2;
-constexpr int MMA_PL = 112;
-static_assert(MMA_SU * MMA_SV <= MMA_PL && MMA_PL % 32 == 16, "stage plane layout");
-constexpr int MMA_STAGE = 12 * MMA_PL;                                   // floats per warp
 
 template <bool SPLIT>
 __global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid g, int side, float memory,
@@ -578,41 +636,7 @@ __global__ void __launch_bounds__(MMA_WARPS * 32) k_lbc_predict_mma(const LGrid 
     if (job >= ntu * ntv) return;                                         // warp-uniform; no block barrier below
     const uint32_t tu = job / ntv, tv = job % ntv;
     const uint32_t cu0 = tu * MMA_TU, cv0 = tv * 16u;                     // first column of the tile (face-local)
-    {
-        // stage: cells (u0 + cu0 - 1 + su, v0 + cv0 - 1 + sv), clamped to the grid like cell_of.
-        // Per (component, su) row of the stage a lane loads the pairs (sv, d) number lane and
-        // lane + 32 of 36, ordered (sv, d) on z faces (the depth pair is contiguous in memory)
-        // and (d, sv) on x and y faces (v = z is contiguous).
-        const int a = f.axis, ua = a == 0 ? 1 : 0, va = a == 2 ? 1 : 2;
-        const uint64_t syz = (uint64_t)g.s[1] * g.s[2];
-        const uint64_t sd = a == 0 ? syz : a == 1 ? (uint64_t)g.s[2] : 1u;     // strides of the depth,
-        const uint64_t sua = ua == 0 ? syz : (uint64_t)g.s[2];                 // u and v axes
-        const uint64_t sva = va == 1 ? (uint64_t)g.s[2] : 1u;
-        uint64_t off[2];
-        int soff[2];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int e = lane + 32 * h < 2 * MMA_SV ? lane + 32 * h : 0;
-            const int d = a == 2 ? (e & 1) : e / MMA_SV;
-            const int sv = a == 2 ? (e >> 1) : e % MMA_SV;
-            const uint32_t cd = f.side ? g.s[a] - 1u - (uint32_t)d : (uint32_t)d;
-            const uint32_t cv = clampu((int)(f.v0 + cv0) - 1 + sv, g.s[va]);
-            off[h] = cd * sd + cv * sva;
-            soff[h] = d * MMA_PL + sv;
-        }
-        const bool second = lane + 32 < 2 * MMA_SV;
-#pragma unroll 1
-        for (int su = 0; su < MMA_SU; ++su) {
-            const uint64_t ou = clampu((int)(f.u0 + cu0) - 1 + su, g.s[ua]) * sua;
-#pragma unroll
-            for (int q = 0; q < 6; ++q) {
-                const float *src = q < 3 ? E + q * g.N : H + (q - 3) * g.N;
-                float *dst = st + q * 2 * MMA_PL + su * MMA_SV;
-                dst[soff[0]] = src[ou + off[0]];
-                if (second) dst[soff[1]] = src[ou + off[1]];
-            }
-        }
-    }
+    stage_tile(g, f, cu0, cv0, E, H, st, lane);
     __syncwarp();
     for (int tr = 0; tr < MMA_TU; ++tr) {
         const uint32_t cu = cu0 + (uint32_t)tr;
@@ -961,12 +985,18 @@ cudaError_t launch_lbc_predict(const LGrid &g, int side, int precision, float me
     for (int f = 0; f < g.nface; ++f) maxc = g.face[f].ncol > maxc ? g.face[f].ncol : maxc;
     if (precision == LBC_F32 || precision == LBC_LINEAR) {
         const dim3 gi((maxc + T_APPLY - 1) / T_APPLY, (unsigned)g.nface, 1);
+        uint32_t maxj = 0;
+        for (int f = 0; f < g.nface; ++f) {
+            const uint32_t nj = ((g.face[f].nu + MMA_TU - 1) / MMA_TU) * ((g.face[f].nv + 15) / 16);
+            maxj = nj > maxj ? nj : maxj;
+        }
         if (precision == LBC_F32) {
             const cudaError_t e = smem_opt_in((const void *)k_lbc_predict32, SMEM_PREDICT32, MLP32_SMEM);
             if (e != cudaSuccess) return e;
             k_lbc_predict32<<<gi, T_APPLY, MLP32_SMEM, st>>>(g, side, memory, (const float *)W, E, H, pred);
         } else {
-            k_lbc_predict_lin<<<gi, T_APPLY, 0, st>>>(g, side, memory, (const float *)W, E, H, pred);
+            const dim3 gl((maxj + MMA_WARPS - 1) / MMA_WARPS, (unsigned)g.nface, 1);
+            k_lbc_predict_lin<<<gl, MMA_WARPS * 32, 0, st>>>(g, side, memory, (const float *)W, E, H, pred);
         }
         return cudaGetLastError();
     }
