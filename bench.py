@@ -560,8 +560,12 @@ def main():
         ms = total / K
         ach = step_bytes / (ms * 1e-3) / 1e9
         nslab = (wl["shape"][0] + sim.slab_planes() - 1) // sim.slab_planes()
+        # per step: the path's kernels, the point-source add (fused: inside k_step) and the
+        # DFT monitor sample when the monitor is timed
         launches = {"fused": K, "hs": 3 * K,
                     "slab": K * ((3 if poynting else 2) * nslab + (3 if poynting else 1) + 1)}[name]
+        if mon is not None and (name == "hs" or (name == "fused" and args.path == "fused")):
+            launches += K
         kname = {"fused": "k_step", "hs": "step (k_bulk_e + k_bulk_hs)",
                  "slab": "step (k_bulk_e/h/s over L2 slabs)"}[name]
         out_paths[name] = {

@@ -238,7 +238,7 @@ int run_update_j(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, double c, d
 }
 
 template <typename R>
-int run_dft(FdtdPlan *p, const void *field, cudaStream_t st, const FdtdDftMonitor *m, int64_t t)
+DftK<R> dft_args(FdtdPlan *p, const void *field, const FdtdDftMonitor *m, int64_t t)
 {
     DftK<R> k;
     k.field = (const R *)field;
@@ -251,14 +251,19 @@ int run_dft(FdtdPlan *p, const void *field, cudaStream_t st, const FdtdDftMonito
     k.step = m->step + t;
     k.series_row = m->series_row + t;
     k.dt = p->d.dt;
-    return check_cuda(launch_dft<R>(k, st), "DFT monitor launch");
+    return k;
 }
 
-// Add the sources whose x plane lies in [xbeg, xend) (all when the range is the grid).
 template <typename R>
-int run_point_sources(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st,
-                      const FdtdPointSources *src, int t, uint32_t xbeg = 0,
-                      uint32_t xend = 0xffffffffu)
+int run_dft(FdtdPlan *p, const void *field, cudaStream_t st, const FdtdDftMonitor *m, int64_t t)
+{
+    return check_cuda(launch_dft<R>(dft_args<R>(p, field, m, t), st), "DFT monitor launch");
+}
+
+// Arguments of the sources whose x plane lies in [xbeg, xend) (all when the range is the grid).
+template <typename R>
+PointK<R> source_args(FdtdPlan *p, const FdtdBuffers *b, const FdtdPointSources *src, int t,
+                      uint32_t xbeg = 0, uint32_t xend = 0xffffffffu)
 {
     PointK<R> k;
     std::memset(&k, 0, sizeof(k));
@@ -275,7 +280,16 @@ int run_point_sources(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st,
         ++n;
     }
     k.n = n;
-    if (!n) return FDTD_OK;
+    return k;
+}
+
+template <typename R>
+int run_point_sources(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st,
+                      const FdtdPointSources *src, int t, uint32_t xbeg = 0,
+                      uint32_t xend = 0xffffffffu)
+{
+    const PointK<R> k = source_args<R>(p, b, src, t, xbeg, xend);
+    if (!k.n) return FDTD_OK;
     return check_cuda(launch_point_sources<R>(k, st), "point source launch");
 }
 
@@ -342,6 +356,16 @@ class KernelTimer {
     cudaEvent_t ev_[MAX_SAMPLES][4];
 };
 
+// The plan's side stream and its two events, created on first use.
+static int side_stream(FdtdPlan *p)
+{
+    if (p->side) return FDTD_OK;
+    int rc;
+    if ((rc = check_cuda(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking), "side stream"))) return rc;
+    if ((rc = check_cuda(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming), "fork event"))) return rc;
+    return check_cuda(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming), "join event");
+}
+
 // Multi-step path with the H+S kernel: update_E in place, point sources, then H and S in one
 // launch that reads H (and the H-side psi) from one copy and writes the other; the copies
 // swap every step and the state is brought home after an odd number of steps.
@@ -384,15 +408,26 @@ int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
     int rc;
     KernelTimer timer(p, nsteps, st);
     if ((rc = timer.init())) return rc;
+    if (mon && (rc = side_stream(p))) return rc;
     for (int t = 0; t < nsteps; ++t) {
         const int a = t & 1, o = a ^ 1;
         bb.H = H[a];
+        // the previous step's DFT sample has read E
+        if (mon && t > 0 && (rc = check_cuda(cudaStreamWaitEvent(st, p->ev_join, 0), "join wait"))) return rc;
         if ((rc = lbc_before_e(p, b, H[a], st))) return rc;
         if ((rc = timer.mark(t, 0))) return rc;
         if ((rc = run_update_e<R>(p, &bb, st, false))) return rc;
         if ((rc = timer.mark(t, 1))) return rc;
         if ((rc = lbc_after_e(p, b, H[a], st))) return rc;
         if (src && src->n > 0 && (rc = run_point_sources<R>(p, &bb, st, src, t))) return rc;
+        // the H+S launch leaves E unchanged: the step's DFT sample runs on the side stream beside
+        // it, and the next step's E update waits for it (below)
+        if (mon) {
+            if ((rc = check_cuda(cudaEventRecord(p->ev_fork, st), "fork event"))) return rc;
+            if ((rc = check_cuda(cudaStreamWaitEvent(p->side, p->ev_fork, 0), "side stream wait"))) return rc;
+            if ((rc = run_dft<R>(p, b->E, p->side, mon, t))) return rc;
+            if ((rc = check_cuda(cudaEventRecord(p->ev_join, p->side), "join event"))) return rc;
+        }
         k.E = (const R *)b->E;
         k.HA = (const R *)H[a];
         k.HB = (R *)H[o];
@@ -412,8 +447,9 @@ int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
         if ((rc = check_cuda(launch_hs<R>(k, p->d.has_mu != 0, dxmode, p->hs_prefetch != 0, st), "H+S launch"))) return rc;
         if ((rc = timer.mark(t, 3))) return rc;
         if ((rc = lbc_after_h(p, b, H[o], st))) return rc;
-        if (mon && (rc = run_dft<R>(p, b->E, st, mon, t))) return rc;
     }
+    // the caller's stream sees the last DFT sample
+    if (mon && nsteps > 0 && (rc = check_cuda(cudaStreamWaitEvent(st, p->ev_join, 0), "join wait"))) return rc;
     if ((rc = timer.finish())) return rc;
     if (nsteps & 1) {
         const size_t fb = 3 * (size_t)p->N * p->elem;
@@ -899,6 +935,9 @@ int fdtd_plan_destroy(FdtdPlan *plan)
     if (!plan) return FDTD_OK;
     if (plan->coef) cudaFree(plan->coef);
     if (plan->status) cudaFree(plan->status);
+    if (plan->ev_fork) cudaEventDestroy(plan->ev_fork);
+    if (plan->ev_join) cudaEventDestroy(plan->ev_join);
+    if (plan->side) cudaStreamDestroy(plan->side);
     delete plan;
     return FDTD_OK;
 }

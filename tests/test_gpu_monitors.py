@@ -131,3 +131,30 @@ def test_monitor_on_own_queue_grows_in_order():
     assert numpy.array_equal(sa, sb)
     assert numpy.array_equal(mon_a.spectrum(), mon_b.spectrum())
     assert numpy.abs(sa).max() > 0
+
+
+def test_dft_monitor_identical_on_every_run_path():
+    """The H+S path takes each step's DFT sample inside its H+S launch (E no longer changes in
+    the step by then); the series and the accumulators equal those of the per-update path and
+    of the one-pass path bit for bit, here with the monitor grown over two runs."""
+    rng = numpy.random.default_rng(21)
+    shape = (14, 12, 10)
+    eps = [rng.uniform(1, 4, shape).astype(numpy.float32) for _ in range(3)]
+    pmls = [{"axis": a, "polarity": p, "thickness": 3} for a in "xyz" for p in "np"]
+    kw = dict(epsilon=eps, pmls=pmls, do_poynting=True)
+    N = int(numpy.prod(shape))
+    n = 24
+    src = [(int(numpy.ravel_multi_index((7, 6, 5), shape)) + N, [math.sin(0.4 * t) for t in range(2 * n)])]
+    pts = [(1, (7, 6, 5)), (0, (2, 3, 4)), (2, (12, 1, 8))]
+    om = numpy.array([0.2, 0.5, 0.9])
+    out = {}
+    for path in ("plain", "hs", "fused"):
+        g = _gpu(**copy.deepcopy(kw))
+        mon = g.dft_monitor(pts, om)
+        g.run(n, point_sources=[(src[0][0], src[0][1][:n])], monitor=mon, path=path)
+        g.run(n, point_sources=[(src[0][0], src[0][1][n:])], monitor=mon, path=path)
+        assert g.tuning("last_run_path") == {"plain": 1, "hs": 2, "fused": 3}[path]
+        out[path] = (mon.series(), mon.spectrum())
+    for path in ("hs", "fused"):
+        assert numpy.array_equal(out[path][0], out["plain"][0]), path
+        assert numpy.array_equal(out[path][1], out["plain"][1]), path
