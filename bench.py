@@ -560,9 +560,10 @@ def main():
         ms = total / K
         ach = step_bytes / (ms * 1e-3) / 1e9
         nslab = (wl["shape"][0] + sim.slab_planes() - 1) // sim.slab_planes()
-        # per step: the path's kernels, the point-source add (fused: inside k_step) and the
-        # DFT monitor sample when the monitor is timed
-        launches = {"fused": K, "hs": 3 * K,
+        # per step: the path's kernels (the workload's one point source is added inside k_step
+        # on the fused path and inside the E kernel on the hs path) and the DFT monitor sample
+        # when the monitor is timed
+        launches = {"fused": K, "hs": 2 * K,
                     "slab": K * ((3 if poynting else 2) * nslab + (3 if poynting else 1) + 1)}[name]
         if mon is not None and (name == "hs" or (name == "fused" and args.path == "fused")):
             launches += K

@@ -138,9 +138,12 @@ YeeK<R> make_yee(const FdtdPlan *p, bool etype, bool imag, R *P, const R *Q, con
     return k;
 }
 
+// With `src` (E only, all planes): the bulk kernel adds the step's point sources itself after
+// the update, when there are at most YEE_SRC of them; *added tells the caller.
 template <typename R>
 int run_update_e(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag,
-                 uint32_t xbeg = 0, uint32_t xend = 0xffffffffu)
+                 uint32_t xbeg = 0, uint32_t xend = 0xffffffffu,
+                 const FdtdPointSources *src = nullptr, int t = 0, bool *added = nullptr)
 {
     R *P = (R *)(imag ? b->F : b->E);
     const R *Q = (const R *)(imag ? b->G : b->H);
@@ -150,6 +153,21 @@ int run_update_e(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag,
                             psi, b->inv_dh);
     k.xbeg = xbeg;
     k.xend = xend < p->sx ? xend : p->sx;
+    if (added) *added = false;
+    if (src && added && !imag && k.bulk && src->n > 0 && src->n <= YEE_SRC && k.xbeg == 0 && k.xend == p->sx) {
+        k.nsrc = src->n;
+        k.src_t = t;
+        k.src_stride = src->n;
+        k.src_values = (const R *)src->values;
+        for (int s = 0; s < src->n; ++s) {
+            const uint64_t ind = (uint64_t)src->index[s], cell = ind % p->N;
+            k.src_c[s] = (int32_t)(ind / p->N);
+            k.src_x[s] = (uint32_t)(cell / p->syz);
+            k.src_j[s] = (uint32_t)(cell % p->syz);
+            k.src_col[s] = s;
+        }
+        *added = true;
+    }
     return check_cuda(launch_yee_e<R>(k, st), imag ? "update_F launch" : "update_E launch");
 }
 
@@ -416,10 +434,13 @@ int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
         if (mon && t > 0 && (rc = check_cuda(cudaStreamWaitEvent(st, p->ev_join, 0), "join wait"))) return rc;
         if ((rc = lbc_before_e(p, b, H[a], st))) return rc;
         if ((rc = timer.mark(t, 0))) return rc;
-        if ((rc = run_update_e<R>(p, &bb, st, false))) return rc;
+        // without a learned boundary (whose E fix-up comes before the sources) the E kernel
+        // adds the point sources itself
+        bool added = false;
+        if ((rc = run_update_e<R>(p, &bb, st, false, 0, 0xffffffffu, p->lbc_mask ? nullptr : src, t, &added))) return rc;
         if ((rc = timer.mark(t, 1))) return rc;
         if ((rc = lbc_after_e(p, b, H[a], st))) return rc;
-        if (src && src->n > 0 && (rc = run_point_sources<R>(p, &bb, st, src, t))) return rc;
+        if (!added && src && src->n > 0 && (rc = run_point_sources<R>(p, &bb, st, src, t))) return rc;
         // the H+S launch leaves E unchanged: the step's DFT sample runs on the side stream beside
         // it, and the next step's E update waits for it (below)
         if (mon) {

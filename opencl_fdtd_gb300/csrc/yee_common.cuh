@@ -62,6 +62,8 @@ struct FaceK {
 //   H-type: P -= dt[/mu] * (curl Q - psi)       (update_h.cl:129-131)
 // coef holds dt/mat precomputed (the same rounded quotient the reference forms per cell);
 // when it is NULL the shell kernels divide. Rp is the other half of Q's complex pair.
+constexpr int YEE_SRC = 8;       // point sources the bulk E kernel can add itself
+
 template <typename R>
 struct YeeK {
     R *P;
@@ -81,6 +83,12 @@ struct YeeK {
     FastDiv dsz;
     int32_t xchunk, bulk;
     uint32_t xbeg, xend;        // planes [xbeg, xend) this launch updates
+    // point sources the bulk E kernel adds after the update, in list order (fdtd.py:168-169):
+    // E[c][x, j] += src_values[src_t * src_stride + src_col] for each of nsrc sources
+    int32_t nsrc, src_t, src_stride, _pad2;
+    const R *src_values;
+    uint32_t src_x[YEE_SRC], src_j[YEE_SRC];
+    int32_t src_c[YEE_SRC], src_col[YEE_SRC];
 };
 
 template <typename R>

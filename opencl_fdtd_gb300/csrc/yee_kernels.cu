@@ -272,6 +272,11 @@ __global__ void __launch_bounds__(EBLOCK, EMINB) k_bulk_e(const YeeK<R> k)
     const FixedFace<R> fz = fixed_face<R, true>(k.ax[2], sz, z);
     R iy = k.inv_d, iz = k.inv_d;
     if (DX == 2) { iy = ldg(k.inv_tab[1] + y); iz = ldg(k.inv_tab[2] + z); }
+    // a point source in this block's cells and planes (block-uniform)
+    bool srcs = false;
+    for (int s = 0; s < k.nsrc; ++s)
+        srcs |= k.src_j[s] / (uint32_t)EBLOCK == blockIdx.x &&
+                (k.src_x[s] - k.xbeg) / (uint32_t)k.xchunk == blockIdx.y;
 
     auto load = [&](uint32_t x, uint32_t i) {
         ELoad<R> v;
@@ -354,9 +359,22 @@ __global__ void __launch_bounds__(EBLOCK, EMINB) k_bulk_e(const YeeK<R> k)
             fz.pu[ip] = su; fz.pv[ip] = sv;
         }
         // update_e.cl:105-107
-        Px[i] = cur.ex + cur.cx * ((d_zy - d_yz) + px);
-        Py[i] = cur.ey + cur.cy * ((d_xz - d_zx) + py);
-        Pz[i] = cur.ez + cur.cz * ((d_yx - d_xy) + pz);
+        R ex = cur.ex + cur.cx * ((d_zy - d_yz) + px);
+        R ey = cur.ey + cur.cy * ((d_xz - d_zx) + py);
+        R ez = cur.ez + cur.cz * ((d_yx - d_xy) + pz);
+        if (srcs) {
+            // the same additions, in list order, as a separate launch after the update
+            for (int s = 0; s < k.nsrc; ++s) {
+                if (k.src_x[s] != x || k.src_j[s] != j) continue;
+                const R val = k.src_values[(int64_t)k.src_t * k.src_stride + k.src_col[s]];
+                if (k.src_c[s] == 0) ex = ex + val;
+                else if (k.src_c[s] == 1) ey = ey + val;
+                else ez = ez + val;
+            }
+        }
+        Px[i] = ex;
+        Py[i] = ey;
+        Pz[i] = ez;
         hy_m = cur.hy;
         hz_m = cur.hz;
         cur = nxt;
