@@ -260,7 +260,10 @@ int fdtd_count_nonfinite(FdtdPlan *plan, const FdtdBuffers *buf, uint32_t *count
  * Bloch boundaries, at most 8 sources, no overlapping CPML faces) each step is two launches
  * (H2 and psi_h2: update_E in place, then H and S) or one (E2, H2 and every psi copy: the
  * one-pass step); oS is then written on the last step only. The path taken is read back with
- * fdtd_plan_get(FDTD_GET_LAST_RUN_PATH). */
+ * fdtd_plan_get(FDTD_GET_LAST_RUN_PATH). On the H+S path the E kernel adds up to 8 point
+ * sources itself (without a learned boundary), and the monitor sample of each step runs on a
+ * stream of the plan beside the H+S launch; that stream is joined back into `stream` before
+ * the call returns, so the caller's stream sees every sample. */
 int fdtd_run(FdtdPlan *plan, const FdtdBuffers *buf, void *stream, int32_t nsteps,
              const FdtdPointSources *src, FdtdDftMonitor *mon);
 
