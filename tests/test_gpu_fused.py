@@ -241,3 +241,31 @@ def test_hs_path_with_mu():
     a.run(21, point_sources=src, path="plain")
     b.run(21, point_sources=src, path="hs")
     _same_state(a, b, True)
+
+
+@pytest.mark.parametrize("kind", ["same_cell", "components", "many"])
+def test_hs_path_point_sources_equal_per_call_loop(kind):
+    """On the H+S path the E kernel adds up to 8 point sources itself (more fall back to the
+    separate launch): repeated sources on one cell component add in list order, sources on
+    the three components of one cell, and 11 sources all give the per-call loop's bits."""
+    rng = numpy.random.default_rng(31)
+    shape = (18, 15, 13)
+    eps = [rng.uniform(1, 4, shape).astype(numpy.float32) for _ in range(3)]
+    pmls = [{"axis": a, "polarity": p, "thickness": 3} for a in "xyz" for p in "np"]
+    kw = dict(epsilon=eps, pmls=pmls, do_poynting=True)
+    N = int(numpy.prod(shape))
+    n = 9
+    cell = int(numpy.ravel_multi_index((9, 7, 6), shape))
+    if kind == "same_cell":
+        inds = [cell + N, cell + N, cell + N]
+    elif kind == "components":
+        inds = [cell, cell + N, cell + 2 * N, cell + N]
+    else:
+        inds = [int(i) for i in rng.integers(0, 3 * N, 11)]
+    src = [(i, [float(rng.standard_normal()) * 10.0 ** -k for _ in range(n)]) for k, i in enumerate(inds)]
+    a = _gpu(**copy.deepcopy(kw))
+    b = _gpu(**copy.deepcopy(kw))
+    a.run(n, point_sources=src, path="plain")
+    b.run(n, point_sources=src, path="hs")
+    assert b.tuning("last_run_path") == 2
+    _same_state(a, b, True)
