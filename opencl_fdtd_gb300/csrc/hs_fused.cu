@@ -21,8 +21,9 @@
 namespace fdtd {
 
 // CPML face of one axis for a cell: depth ir (-1 outside) and side (0 = 'n', 1 = 'p').
-// Coefficients, thickness and psi pointers are read from the launch parameters on use, so a
-// face costs two registers.
+// Thickness and psi pointers are read from the launch parameters on use; the coefficients of
+// a thread's y and z faces, fixed for its march, are loaded once into registers (cy, cz),
+// those of the x face on use.
 struct HSF {
     int ir, side;
 };
@@ -115,7 +116,8 @@ __device__ __forceinline__ void hs_load(const HSK<R> &k, uint32_t x, uint32_t i,
 template <typename R, int DX, bool MU>
 __device__ __forceinline__ void hs_math(const HSK<R> &k, uint32_t x, uint32_t y, uint32_t z,
                                         uint32_t i, const HSF &fx, const HSF &fy,
-                                        const HSF &fz, const HSLoad<R> &v, bool wr, R *os)
+                                        const HSF &fz, const HSLoad<R> &v, bool wr, R *os,
+                                        const R *cy, const R *cz)
 {
     R d_xy = v.rxy - v.ex;
     R d_xz = v.rxz - v.ex;
@@ -145,8 +147,7 @@ __device__ __forceinline__ void hs_math(const HSK<R> &k, uint32_t x, uint32_t y,
     if (fy.ir >= 0) {
         const HSAxis<R> &a = k.ax[1];
         R su, sv;
-        face_update<R, false, 1>(ldg(hs_tab(a, fy, 0) + fy.ir), ldg(hs_tab(a, fy, 1) + fy.ir),
-                                  ldg(hs_tab(a, fy, 2) + fy.ir), v.yu, v.yv, su, sv,
+        face_update<R, false, 1>(cy[0], cy[1], cy[2], v.yu, v.yv, su, sv,
                                   d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
         if (wr) {
             const uint32_t ip = psi_index<1>((uint32_t)fy.ir, hs_T(a, fy), x, y, z, k.sy, k.sz);
@@ -157,8 +158,7 @@ __device__ __forceinline__ void hs_math(const HSK<R> &k, uint32_t x, uint32_t y,
     if (fz.ir >= 0) {
         const HSAxis<R> &a = k.ax[2];
         R su, sv;
-        face_update<R, false, 2>(ldg(hs_tab(a, fz, 0) + fz.ir), ldg(hs_tab(a, fz, 1) + fz.ir),
-                                  ldg(hs_tab(a, fz, 2) + fz.ir), v.zu, v.zv, su, sv,
+        face_update<R, false, 2>(cz[0], cz[1], cz[2], v.zu, v.zv, su, sv,
                                   d_xy, d_xz, d_yx, d_yz, d_zx, d_zy, px, py, pz);
         if (wr) {
             const uint32_t ip = psi_index<2>((uint32_t)fz.ir, hs_T(a, fz), x, y, z, k.sy, k.sz);
@@ -223,6 +223,12 @@ __global__ void __launch_bounds__(HS_THREADS, PF ? 1 : 2) k_bulk_hs(const HSK<R>
     const uint32_t dpz = (z + 1u < sz) ? 1u : 0u - (sz - 1u);
     const HSF fy = hs_face<R>(k.ax[1], sy, y);
     const HSF fz = hs_face<R>(k.ax[2], sz, z);
+    // CPML coefficients of the thread's y and z faces, fixed for the march
+    R cy[3] = {R(0), R(0), R(0)}, cz[3] = {R(0), R(0), R(0)};
+    if (fy.ir >= 0)
+        for (int c = 0; c < 3; ++c) cy[c] = ldg(hs_tab(k.ax[1], fy, c) + fy.ir);
+    if (fz.ir >= 0)
+        for (int c = 0; c < 3; ++c) cz[c] = ldg(hs_tab(k.ax[2], fz, c) + fz.ir);
 
     R prev_yx = R(0), prev_zx = R(0);
     if (own) {
@@ -233,7 +239,7 @@ __global__ void __launch_bounds__(HS_THREADS, PF ? 1 : 2) k_bulk_hs(const HSK<R>
         HSLoad<R> v;
         hs_load<R, MU>(k, xp, ip, dpy, dpz, fx, fy, fz, y, z, v);
         R os[6];
-        hs_math<R, DX, MU>(k, xp, y, z, ip, fx, fy, fz, v, false, os);
+        hs_math<R, DX, MU>(k, xp, y, z, ip, fx, fy, fz, v, false, os, cy, cz);
         prev_yx = os[4];
         prev_zx = os[2];
     }
@@ -247,7 +253,7 @@ __global__ void __launch_bounds__(HS_THREADS, PF ? 1 : 2) k_bulk_hs(const HSK<R>
         if (act) {
             if (PF && x + 1u < xb) hs_load<R, MU>(k, x + 1u, i + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, nxt);
             R os[6];
-            hs_math<R, DX, MU>(k, x, y, z, i, fx, fy, fz, cur, own, os);
+            hs_math<R, DX, MU>(k, x, y, z, i, fx, fy, fz, cur, own, os, cy, cz);
 #pragma unroll
             for (int c = 0; c < 6; ++c) sS[slot][c][t] = os[c];
             if (own && k.write_oS) {
