@@ -562,10 +562,12 @@ def main():
         nslab = (wl["shape"][0] + sim.slab_planes() - 1) // sim.slab_planes()
         # per step: the path's kernels (the workload's one point source is added inside k_step
         # on the fused path and inside the E kernel on the hs path) and the DFT monitor sample
-        # when the monitor is timed
+        # when the monitor is timed (on the hs path by one block of the H+S launch unless the
+        # plan's hs_dft is off)
         launches = {"fused": K, "hs": 2 * K,
                     "slab": K * ((3 if poynting else 2) * nslab + (3 if poynting else 1) + 1)}[name]
-        if mon is not None and (name == "hs" or (name == "fused" and args.path == "fused")):
+        if mon is not None and ((name == "hs" and not sim.tuning("hs_dft"))
+                                or (name == "fused" and args.path == "fused")):
             launches += K
         kname = {"fused": "k_step", "hs": "step (k_bulk_e + k_bulk_hs)",
                  "slab": "step (k_bulk_e/h/s over L2 slabs)"}[name]
@@ -595,6 +597,10 @@ def main():
     head = min(cands, key=lambda n: out_paths[n]["ms_per_step"]) if cands else "dropin"
     hp = out_paths[head]
     step_gbs = step_bytes / (hp["ms_per_step"] * 1e-3) / 1e9
+    # launch options of the H+S path as the timed run used them
+    launch = ({"hs_xchunk": sim.tuning("hs_xchunk_used"), "pdl": sim.tuning("pdl"),
+               "dft_in_hs_launch": sim.tuning("hs_dft"), "e_xchunk": sim.tuning("xchunk")}
+              if head == "hs" else None)
 
     e2e = None
     if not args.no_e2e:
@@ -633,6 +639,7 @@ def main():
                                 "slab": "Simulation.run(path='plain'): E, point source, H, S update kernels",
                                 "dropin": "per-call update_E / source add / update_H / update_S"}[head],
             "parallelism": "replicas" if world > 1 else "single GPU",
+            "launch": launch,
             "monitor": mon_out,
             # the dominant kernel's roofline: per-call timing of the same kernels the run
             # path launches (the fused path reports its own kernel)

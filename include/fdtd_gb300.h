@@ -135,11 +135,21 @@ int fdtd_plan_destroy(FdtdPlan *plan);
  *   FUSED_SHAPE   block shape of the one-pass step: 1 large (up to 1024 threads, one block per
  *                 SM), 2 small (up to 512 threads, two blocks per SM; float32 only), 0
  *                 (default) small when its tiles hold at least 3 own rows
- *   HS_XCHUNK     x planes one block of the H+S kernel of fdtd_run marches (default 16)
+ *   HS_XCHUNK     x planes one block of the H+S kernel of fdtd_run marches; 0 (default): chosen
+ *                 per launch among 14..24 so that the grid best fills whole waves of resident
+ *                 blocks (18 on the 395x345x73 grid of a 152-SM GPU)
  *   HS_PREFETCH   1: the H+S kernel loads the next plane ahead (one block per SM); 0: not
  *                 (two blocks per SM, the default)
  *   HS_REVERSE    1 (default): the H+S kernel takes its x chunks in descending order, so that it
  *                 starts on the planes update_E wrote last (still in L2); 0: ascending
+ *   HS_PLANES     x planes the H+S kernel evaluates per block barrier: 1 (default) or 2 (float
+ *                 only; double takes 1)
+ *   HS_DFT        1 (default): on the H+S path the step's DFT monitor sample is taken by one extra
+ *                 block of the H+S launch; 0: by the monitor kernel on a side stream beside it
+ *   PDL           1 (default): on the H+S path the E and H+S kernels are launched with
+ *                 programmatic stream serialization (each may be scheduled while the kernel
+ *                 before it finishes, and waits for it before touching memory); 0: plain stream
+ *                 order
  *   TIMING        1: fdtd_run records CUDA events around its kernels on up to 64 steps spread
  *                 over the call (update_E and H+S on the H+S path, the step kernel on the
  *                 one-pass path) and waits for the stream before it returns (profiling; read
@@ -155,14 +165,19 @@ int fdtd_plan_destroy(FdtdPlan *plan);
 #define FDTD_TUNE_FUSED_TMA 9
 #define FDTD_TUNE_FUSED_SHAPE 10
 #define FDTD_TUNE_HS_REVERSE 11
-/* Read-only keys of fdtd_plan_get: the path of the last fdtd_run (FDTD_PATH_*) and the tiling
- * of its last one-pass launch (own rows per tile, x chunk, stages, threads per block, shape). */
+#define FDTD_TUNE_HS_PLANES 12
+#define FDTD_TUNE_HS_DFT 13
+#define FDTD_TUNE_PDL 14
+/* Read-only keys of fdtd_plan_get: the path of the last fdtd_run (FDTD_PATH_*), the tiling
+ * of its last one-pass launch (own rows per tile, x chunk, stages, threads per block, shape)
+ * and the x chunk of its last H+S launch. */
 #define FDTD_GET_LAST_RUN_PATH 100
 #define FDTD_GET_STEP_ROWS 101
 #define FDTD_GET_STEP_XCHUNK 102
 #define FDTD_GET_STEP_STAGES 103
 #define FDTD_GET_STEP_THREADS 104
 #define FDTD_GET_STEP_SHAPE 105
+#define FDTD_GET_HS_XCHUNK_USED 106
 #define FDTD_PATH_NONE 0
 #define FDTD_PATH_PER_UPDATE 1     /* update_E, sources, update_H, update_S launches */
 #define FDTD_PATH_HS 2             /* update_E in place, sources, H and S in one launch */
@@ -261,9 +276,10 @@ int fdtd_count_nonfinite(FdtdPlan *plan, const FdtdBuffers *buf, uint32_t *count
  * (H2 and psi_h2: update_E in place, then H and S) or one (E2, H2 and every psi copy: the
  * one-pass step); oS is then written on the last step only. The path taken is read back with
  * fdtd_plan_get(FDTD_GET_LAST_RUN_PATH). On the H+S path the E kernel adds up to 8 point
- * sources itself (without a learned boundary), and the monitor sample of each step runs on a
- * stream of the plan beside the H+S launch; that stream is joined back into `stream` before
- * the call returns, so the caller's stream sees every sample. */
+ * sources itself (without a learned boundary), the monitor sample of each step is taken by
+ * one extra block of the H+S launch (FDTD_TUNE_HS_DFT; 0: by the monitor kernel on a stream of
+ * the plan beside the H+S launch, joined back into `stream` before the call returns), and the
+ * two kernels use programmatic dependent launch (FDTD_TUNE_PDL). */
 int fdtd_run(FdtdPlan *plan, const FdtdBuffers *buf, void *stream, int32_t nsteps,
              const FdtdPointSources *src, FdtdDftMonitor *mon);
 

@@ -34,12 +34,16 @@ FDTD_TUNE_FUSED_STAGES = 8
 FDTD_TUNE_FUSED_TMA = 9
 FDTD_TUNE_FUSED_SHAPE = 10
 FDTD_TUNE_HS_REVERSE = 11
+FDTD_TUNE_HS_PLANES = 12
+FDTD_TUNE_HS_DFT = 13
+FDTD_TUNE_PDL = 14
 FDTD_GET_LAST_RUN_PATH = 100
 FDTD_GET_STEP_ROWS = 101
 FDTD_GET_STEP_XCHUNK = 102
 FDTD_GET_STEP_STAGES = 103
 FDTD_GET_STEP_THREADS = 104
 FDTD_GET_STEP_SHAPE = 105
+FDTD_GET_HS_XCHUNK_USED = 106
 FDTD_PATH_NONE = 0
 FDTD_PATH_PER_UPDATE = 1
 FDTD_PATH_HS = 2

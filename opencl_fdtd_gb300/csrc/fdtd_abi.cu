@@ -6,6 +6,7 @@
 // source switches. The kernels are compiled once for every combination instead of being
 // rendered per simulation; the plan only fills their argument blocks.
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -143,7 +144,8 @@ YeeK<R> make_yee(const FdtdPlan *p, bool etype, bool imag, R *P, const R *Q, con
 template <typename R>
 int run_update_e(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag,
                  uint32_t xbeg = 0, uint32_t xend = 0xffffffffu,
-                 const FdtdPointSources *src = nullptr, int t = 0, bool *added = nullptr)
+                 const FdtdPointSources *src = nullptr, int t = 0, bool *added = nullptr,
+                 bool pdl = false)
 {
     R *P = (R *)(imag ? b->F : b->E);
     const R *Q = (const R *)(imag ? b->G : b->H);
@@ -168,7 +170,7 @@ int run_update_e(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, bool imag,
         }
         *added = true;
     }
-    return check_cuda(launch_yee_e<R>(k, st), imag ? "update_F launch" : "update_E launch");
+    return check_cuda(launch_yee_e<R>(k, st, pdl), imag ? "update_F launch" : "update_E launch");
 }
 
 template <typename R>
@@ -384,6 +386,29 @@ static int side_stream(FdtdPlan *p)
     return check_cuda(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming), "join event");
 }
 
+// x chunk of the H+S kernel when none is set: among 14..24 planes, the one whose grid (plus
+// the extra blocks) best fills whole waves of resident blocks, two per SM; the smallest such
+// chunk on a tie. On the 395x345x73 grid (69 row blocks, 152 SMs) it is 18: 1518 blocks, 4.99
+// waves, which ran 2% faster per step than 16 planes (5.67 waves).
+static uint32_t hs_auto_xchunk(const FdtdPlan *p, uint32_t nrowblk, uint32_t extra)
+{
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess || nsm <= 0)
+        nsm = 1;
+    const double slots = 2.0 * nsm;
+    uint32_t best = 16;
+    double best_eff = -1.0;
+    for (uint32_t xc = 14; xc <= 24; ++xc) {
+        const double waves = (double)(nrowblk * ((p->sx + xc - 1u) / xc) + extra) / slots;
+        const double eff = waves / std::ceil(waves);
+        if (eff > best_eff + 1e-12) {
+            best_eff = eff;
+            best = xc;
+        }
+    }
+    return best;
+}
+
 // Multi-step path with the H+S kernel: update_E in place, point sources, then H and S in one
 // launch that reads H (and the H-side psi) from one copy and writes the other; the copies
 // swap every step and the state is brought home after an odd number of steps.
@@ -409,7 +434,10 @@ int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
     k.dsz = FastDiv::make(p->sz);
     k.rows = (uint32_t)HS_THREADS / p->sz - 1u;
     k.reverse = p->hs_reverse;
-    k.xchunk = p->hs_xchunk;
+    k.nrowblk = (k.sy + k.rows - 1u) / k.rows;
+    k.xchunk = p->hs_xchunk ? p->hs_xchunk : hs_auto_xchunk(p, k.nrowblk, mon && p->hs_dft ? 1u : 0u);
+    k.nchunk = (k.sx + k.xchunk - 1u) / k.xchunk;
+    p->hs_xchunk_used = (int32_t)k.xchunk;
     int fidx[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
     for (int f = 0; f < p->d.n_pml; ++f) {
         const FdtdPmlDesc &pd = p->d.pml[f];
@@ -426,24 +454,30 @@ int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
     int rc;
     KernelTimer timer(p, nsteps, st);
     if ((rc = timer.init())) return rc;
-    if (mon && (rc = side_stream(p))) return rc;
+    // the step's DFT sample: in the H+S launch (one extra block) or on the side stream beside it
+    const bool dft_in = mon && p->hs_dft;
+    const bool dft_side = mon && !p->hs_dft;
+    const bool pdl = p->pdl != 0;
+    if (dft_side && (rc = side_stream(p))) return rc;
     for (int t = 0; t < nsteps; ++t) {
         const int a = t & 1, o = a ^ 1;
         bb.H = H[a];
         // the previous step's DFT sample has read E
-        if (mon && t > 0 && (rc = check_cuda(cudaStreamWaitEvent(st, p->ev_join, 0), "join wait"))) return rc;
+        if (dft_side && t > 0 && (rc = check_cuda(cudaStreamWaitEvent(st, p->ev_join, 0), "join wait"))) return rc;
         if ((rc = lbc_before_e(p, b, H[a], st))) return rc;
         if ((rc = timer.mark(t, 0))) return rc;
         // without a learned boundary (whose E fix-up comes before the sources) the E kernel
         // adds the point sources itself
         bool added = false;
-        if ((rc = run_update_e<R>(p, &bb, st, false, 0, 0xffffffffu, p->lbc_mask ? nullptr : src, t, &added))) return rc;
+        if ((rc = run_update_e<R>(p, &bb, st, false, 0, 0xffffffffu, p->lbc_mask ? nullptr : src, t, &added, pdl))) return rc;
         if ((rc = timer.mark(t, 1))) return rc;
         if ((rc = lbc_after_e(p, b, H[a], st))) return rc;
         if (!added && src && src->n > 0 && (rc = run_point_sources<R>(p, &bb, st, src, t))) return rc;
         // the H+S launch leaves E unchanged: the step's DFT sample runs on the side stream beside
         // it, and the next step's E update waits for it (below)
-        if (mon) {
+        k.dft_on = dft_in ? 1 : 0;
+        if (dft_in) k.dft = dft_args<R>(p, b->E, mon, t);
+        if (dft_side) {
             if ((rc = check_cuda(cudaEventRecord(p->ev_fork, st), "fork event"))) return rc;
             if ((rc = check_cuda(cudaStreamWaitEvent(p->side, p->ev_fork, 0), "side stream wait"))) return rc;
             if ((rc = run_dft<R>(p, b->E, p->side, mon, t))) return rc;
@@ -465,12 +499,12 @@ int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
             }
         k.write_oS = t == nsteps - 1;
         if ((rc = timer.mark(t, 2))) return rc;
-        if ((rc = check_cuda(launch_hs<R>(k, p->d.has_mu != 0, dxmode, p->hs_prefetch != 0, st), "H+S launch"))) return rc;
+        if ((rc = check_cuda(launch_hs<R>(k, p->d.has_mu != 0, dxmode, p->hs_prefetch != 0, p->hs_planes, pdl, st), "H+S launch"))) return rc;
         if ((rc = timer.mark(t, 3))) return rc;
         if ((rc = lbc_after_h(p, b, H[o], st))) return rc;
     }
     // the caller's stream sees the last DFT sample
-    if (mon && nsteps > 0 && (rc = check_cuda(cudaStreamWaitEvent(st, p->ev_join, 0), "join wait"))) return rc;
+    if (dft_side && nsteps > 0 && (rc = check_cuda(cudaStreamWaitEvent(st, p->ev_join, 0), "join wait"))) return rc;
     if ((rc = timer.finish())) return rc;
     if (nsteps & 1) {
         const size_t fb = 3 * (size_t)p->N * p->elem;
@@ -899,9 +933,13 @@ int fdtd_plan_create(const FdtdDesc *desc, FdtdPlan **out)
     p->fused_shape = 0;
     p->last_run_path = FDTD_PATH_NONE;
     std::memset(p->step_cfg, 0, sizeof(p->step_cfg));
-    p->hs_xchunk = 16;
+    p->hs_xchunk = 0;
     p->hs_prefetch = 0;
     p->hs_reverse = 1;
+    p->hs_planes = 1;
+    p->hs_xchunk_used = 0;
+    p->hs_dft = 1;
+    p->pdl = 1;
     p->timing = 0;
     p->kernel_ms[0] = p->kernel_ms[1] = 0.0;
     p->kernel_samples = 0;
@@ -1001,7 +1039,7 @@ int fdtd_plan_tune(FdtdPlan *p, int32_t key, int32_t value)
         p->fused_shape = value;
         return FDTD_OK;
     case FDTD_TUNE_HS_XCHUNK:
-        if (value < 1 || value > 4096) return fail(FDTD_ERR_INVALID, "hs_xchunk must be in [1, 4096]");
+        if (value < 0 || value > 4096) return fail(FDTD_ERR_INVALID, "hs_xchunk must be in [0, 4096] (0: automatic)");
         p->hs_xchunk = (uint32_t)value;
         return FDTD_OK;
     case FDTD_TUNE_TIMING:
@@ -1011,6 +1049,18 @@ int fdtd_plan_tune(FdtdPlan *p, int32_t key, int32_t value)
     case FDTD_TUNE_HS_PREFETCH:
         if (value != 0 && value != 1) return fail(FDTD_ERR_INVALID, "hs_prefetch must be 0 or 1");
         p->hs_prefetch = value;
+        return FDTD_OK;
+    case FDTD_TUNE_HS_PLANES:
+        if (value != 1 && value != 2) return fail(FDTD_ERR_INVALID, "hs_planes must be 1 or 2");
+        p->hs_planes = value;
+        return FDTD_OK;
+    case FDTD_TUNE_HS_DFT:
+        if (value != 0 && value != 1) return fail(FDTD_ERR_INVALID, "hs_dft must be 0 or 1");
+        p->hs_dft = value;
+        return FDTD_OK;
+    case FDTD_TUNE_PDL:
+        if (value != 0 && value != 1) return fail(FDTD_ERR_INVALID, "pdl must be 0 or 1");
+        p->pdl = value;
         return FDTD_OK;
     default:
         return fail(FDTD_ERR_INVALID, "unknown tuning key");
@@ -1037,6 +1087,10 @@ int fdtd_plan_get(const FdtdPlan *p, int32_t key, int32_t *value)
     case FDTD_GET_STEP_THREADS: *value = p->step_cfg[3]; return FDTD_OK;
     case FDTD_TUNE_HS_XCHUNK: *value = (int32_t)p->hs_xchunk; return FDTD_OK;
     case FDTD_TUNE_HS_PREFETCH: *value = p->hs_prefetch; return FDTD_OK;
+    case FDTD_TUNE_HS_PLANES: *value = p->hs_planes; return FDTD_OK;
+    case FDTD_GET_HS_XCHUNK_USED: *value = p->hs_xchunk_used; return FDTD_OK;
+    case FDTD_TUNE_HS_DFT: *value = p->hs_dft; return FDTD_OK;
+    case FDTD_TUNE_PDL: *value = p->pdl; return FDTD_OK;
     case FDTD_TUNE_TIMING: *value = p->timing; return FDTD_OK;
     default: return fail(FDTD_ERR_INVALID, "unknown tuning key");
     }

@@ -191,22 +191,56 @@ __device__ __forceinline__ void hs_math(const HSK<R> &k, uint32_t x, uint32_t y,
     os[5] = (-(v.ryz + v.ey)) * ahx;
 }
 
+// S at the cell of thread t from the products of one plane in shared memory (six planes of
+// HS_THREADS values: xy, yz, zx, xz, yx, zy) and the thread's x-1 products (update_s.cl:33-36);
+// the x-1 products become this plane's.
+template <typename R>
+__device__ __forceinline__ void hs_s(const HSK<R> &k, const R *q, uint32_t t, uint32_t z,
+                                     uint32_t i, R &prev_yx, R &prev_zx)
+{
+    const uint64_t N = k.N;
+    const uint32_t sz = k.sz;
+    const uint32_t tz = z ? t - 1u : t + sz - 1u;  // z-1, wrapped within the row
+    const R a_xy = q[t], a_yz = q[HS_THREADS + t], a_zx = q[2 * HS_THREADS + t];
+    const R a_xz = q[3 * HS_THREADS + t], a_yx = q[4 * HS_THREADS + t], a_zy = q[5 * HS_THREADS + t];
+    const R xy_y = q[t - sz], zy_y = q[5 * HS_THREADS + t - sz];
+    const R xz_z = q[3 * HS_THREADS + tz], yz_z = q[HS_THREADS + tz];
+    k.S[i] = (((a_xy + a_xz) + xy_y) + xz_z) * k.sf;
+    k.S[N + i] = (((a_yz + a_yx) + yz_z) + prev_yx) * k.sf;
+    k.S[2 * N + i] = (((a_zx + a_zy) + prev_zx) + zy_y) * k.sf;
+    prev_yx = a_yx;
+    prev_zx = a_zx;
+}
+
 // Thread t of a block works on window row w = t / sz (cell z = t % sz): row 0 is the halo row
 // y0 - 1 (wrapped), whose products only feed S of row y0; rows 1..rows are the block's own
-// rows y0 .. y0 + rows - 1. Every thread evaluates exactly one cell per plane, so the single
-// barrier per plane waits for no extra work. The products go to shared memory slots that
-// alternate by plane, which is what lets one barrier per plane suffice.
+// rows y0 .. y0 + rows - 1. Every thread evaluates exactly one cell per plane, so a barrier
+// waits for no extra work. The products of PB consecutive planes go to shared memory slots,
+// then one barrier, then S of those planes; the slot groups alternate, which is what lets one
+// barrier per PB planes suffice.
 // PF: issue the next plane's loads before the current plane's arithmetic (one block per SM
 // with room for both sets of registers); otherwise (two blocks per SM) they are issued after
-// the products are stored, so they are in flight during the barrier and the S assembly.
-template <typename R, int DX, bool MU, bool PF>
+// the products are stored, so that the last plane's are in flight during the barrier and the
+// S assembly.
+// The grid is one-dimensional: block b takes row block b % nrowblk and x chunk b / nrowblk (row
+// blocks fastest). With dft_on one more block (the last) takes the step's DFT monitor sample
+// of E, which this launch leaves unchanged; a single block keeps a grid that fills whole
+// waves of resident blocks doing so.
+template <typename R, int DX, bool MU, bool PF, int PB>
 __global__ void __launch_bounds__(HS_THREADS, PF ? 1 : 2) k_bulk_hs(const HSK<R> k)
 {
-    __shared__ R sS[2][6][HS_THREADS];
+    __shared__ R sS[2 * PB][6][HS_THREADS];
+    grid_dependency_sync();
     const uint32_t t = threadIdx.x;
+    const uint32_t chunk = blockIdx.x / k.nrowblk;
+    if (chunk >= k.nchunk) {
+        const int nq = k.dft.npoint * (k.dft.nfreq > 0 ? k.dft.nfreq : 1);
+        for (int q = (int)t; q < nq; q += HS_THREADS) dft_sample(k.dft, q);
+        return;
+    }
     const uint32_t sx = k.sx, sy = k.sy, sz = k.sz, syz = k.syz;
     const uint64_t N = k.N;
-    const uint32_t y0 = blockIdx.x * k.rows;
+    const uint32_t y0 = (blockIdx.x - chunk * k.nrowblk) * k.rows;
     const uint32_t nrow = min(k.rows, sy - y0);
     const bool act = t < (nrow + 1u) * sz;
     const uint32_t w = act ? k.dsz.div(t) : 0u;
@@ -216,7 +250,7 @@ __global__ void __launch_bounds__(HS_THREADS, PF ? 1 : 2) k_bulk_hs(const HSK<R>
     const uint32_t j = y * sz + z;
     // chunks in descending x order start where the preceding update_E (ascending) finished, on
     // planes still in L2
-    const uint32_t xa = (k.reverse ? gridDim.y - 1u - blockIdx.y : blockIdx.y) * k.xchunk;
+    const uint32_t xa = (k.reverse ? k.nchunk - 1u - chunk : chunk) * k.xchunk;
     const uint32_t xb = min(xa + k.xchunk, sx);
     // plus neighbours (common.cl:82-84) in 32-bit wrap arithmetic
     const uint32_t dpy = (y + 1u < sy) ? sz : 0u - (sy - 1u) * sz;
@@ -246,68 +280,101 @@ __global__ void __launch_bounds__(HS_THREADS, PF ? 1 : 2) k_bulk_hs(const HSK<R>
     HSLoad<R> cur;
     uint32_t i = xa * syz + j;
     if (act) hs_load<R, MU>(k, xa, i, dpy, dpz, hs_face<R>(k.ax[0], sx, xa), fy, fz, y, z, cur);
-    for (uint32_t x = xa; x < xb; ++x, i += syz) {
-        const HSF fx = hs_face<R>(k.ax[0], sx, x);
-        const int slot = (int)(x & 1u);
-        HSLoad<R> nxt;
-        if (act) {
-            if (PF && x + 1u < xb) hs_load<R, MU>(k, x + 1u, i + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, nxt);
-            R os[6];
-            hs_math<R, DX, MU>(k, x, y, z, i, fx, fy, fz, cur, own, os, cy, cz);
+    if constexpr (PB == 1) {
+        for (uint32_t x = xa; x < xb; ++x, i += syz) {
+            const HSF fx = hs_face<R>(k.ax[0], sx, x);
+            const int slot = (int)(x & 1u);
+            HSLoad<R> nxt;
+            if (act) {
+                if (PF && x + 1u < xb) hs_load<R, MU>(k, x + 1u, i + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, nxt);
+                R os[6];
+                hs_math<R, DX, MU>(k, x, y, z, i, fx, fy, fz, cur, own, os, cy, cz);
 #pragma unroll
-            for (int c = 0; c < 6; ++c) sS[slot][c][t] = os[c];
-            if (own && k.write_oS) {
+                for (int c = 0; c < 6; ++c) sS[slot][c][t] = os[c];
+                if (own && k.write_oS) {
 #pragma unroll
-                for (int c = 0; c < 6; ++c) k.oS[(uint64_t)c * N + i] = os[c];
+                    for (int c = 0; c < 6; ++c) k.oS[(uint64_t)c * N + i] = os[c];
+                }
+                // the next plane's loads fly during the barrier and the S assembly
+                if (!PF && x + 1u < xb)
+                    hs_load<R, MU>(k, x + 1u, i + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, cur);
             }
-            // the next plane's loads fly during the barrier and the S assembly
-            if (!PF && x + 1u < xb)
-                hs_load<R, MU>(k, x + 1u, i + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, cur);
+            __syncthreads();
+            if (own) hs_s<R>(k, sS[slot][0], t, z, i, prev_yx, prev_zx);
+            if (PF && act) cur = nxt;
         }
-        __syncthreads();
-        if (own) {
-            const R *q = &sS[slot][0][0];
-            const uint32_t tz = z ? t - 1u : t + sz - 1u;  // z-1, wrapped within the row
-            const R a_xy = q[t], a_yz = q[HS_THREADS + t], a_zx = q[2 * HS_THREADS + t];
-            const R a_xz = q[3 * HS_THREADS + t], a_yx = q[4 * HS_THREADS + t], a_zy = q[5 * HS_THREADS + t];
-            const R xy_y = q[t - sz], zy_y = q[5 * HS_THREADS + t - sz];
-            const R xz_z = q[3 * HS_THREADS + tz], yz_z = q[HS_THREADS + tz];
-            // update_s.cl:33-36
-            k.S[i] = (((a_xy + a_xz) + xy_y) + xz_z) * k.sf;
-            k.S[N + i] = (((a_yz + a_yx) + yz_z) + prev_yx) * k.sf;
-            k.S[2 * N + i] = (((a_zx + a_zy) + prev_zx) + zy_y) * k.sf;
-            prev_yx = a_yx;
-            prev_zx = a_zx;
+    } else {
+        for (uint32_t xg = xa; xg < xb; xg += PB, i += PB * syz) {
+            // slot group: xg / PB advances by one per group, so the groups alternate
+            const int base = (int)((xg / (uint32_t)PB) & 1u) * PB;
+#pragma unroll
+            for (int p = 0; p < PB; ++p) {
+                const uint32_t x = xg + (uint32_t)p;
+                if (x >= xb) break;   // block-uniform
+                const uint32_t ix = i + (uint32_t)p * syz;
+                if (act) {
+                    const HSF fx = hs_face<R>(k.ax[0], sx, x);
+                    HSLoad<R> nxt;
+                    if (PF && x + 1u < xb) hs_load<R, MU>(k, x + 1u, ix + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, nxt);
+                    R os[6];
+                    hs_math<R, DX, MU>(k, x, y, z, ix, fx, fy, fz, cur, own, os, cy, cz);
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) sS[base + p][c][t] = os[c];
+                    if (own && k.write_oS) {
+#pragma unroll
+                        for (int c = 0; c < 6; ++c) k.oS[(uint64_t)c * N + ix] = os[c];
+                    }
+                    // the next plane's loads (those of the group's last plane fly during the
+                    // barrier and the S assembly)
+                    if (!PF && x + 1u < xb)
+                        hs_load<R, MU>(k, x + 1u, ix + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, cur);
+                    if (PF) cur = nxt;
+                }
+            }
+            __syncthreads();
+            if (own) {
+#pragma unroll
+                for (int p = 0; p < PB; ++p) {
+                    if (xg + (uint32_t)p >= xb) break;
+                    hs_s<R>(k, sS[base + p][0], t, z, i + (uint32_t)p * syz, prev_yx, prev_zx);
+                }
+            }
         }
-        if (PF && act) cur = nxt;
     }
 }
 
-template <typename R, int DX, bool PF>
-static void launch_hs_dx(const HSK<R> &k, bool mu, dim3 g, cudaStream_t st)
+template <typename R, int DX, bool PF, int PB>
+static cudaError_t launch_hs_dx(const HSK<R> &k, bool mu, dim3 g, bool pdl, cudaStream_t st)
 {
-    if (mu) k_bulk_hs<R, DX, true, PF><<<g, HS_THREADS, 0, st>>>(k);
-    else k_bulk_hs<R, DX, false, PF><<<g, HS_THREADS, 0, st>>>(k);
+    if (mu) return launch_dependent(k_bulk_hs<R, DX, true, PF, PB>, g, HS_THREADS, st, pdl, k);
+    return launch_dependent(k_bulk_hs<R, DX, false, PF, PB>, g, HS_THREADS, st, pdl, k);
 }
 
-template <typename R, bool PF>
-static void launch_hs_pf(const HSK<R> &k, bool mu, int dxmode, dim3 g, cudaStream_t st)
+template <typename R, bool PF, int PB>
+static cudaError_t launch_hs_pf(const HSK<R> &k, bool mu, int dxmode, dim3 g, bool pdl, cudaStream_t st)
 {
-    if (dxmode == 0) launch_hs_dx<R, 0, PF>(k, mu, g, st);
-    else if (dxmode == 1) launch_hs_dx<R, 1, PF>(k, mu, g, st);
-    else launch_hs_dx<R, 2, PF>(k, mu, g, st);
+    if (dxmode == 0) return launch_hs_dx<R, 0, PF, PB>(k, mu, g, pdl, st);
+    if (dxmode == 1) return launch_hs_dx<R, 1, PF, PB>(k, mu, g, pdl, st);
+    return launch_hs_dx<R, 2, PF, PB>(k, mu, g, pdl, st);
 }
 
 template <typename R>
-cudaError_t launch_hs(const HSK<R> &k, bool mu, int dxmode, bool prefetch, cudaStream_t st)
+cudaError_t launch_hs(const HSK<R> &k, bool mu, int dxmode, bool prefetch, int planes, bool pdl,
+                      cudaStream_t st)
 {
-    const dim3 g((k.sy + k.rows - 1) / k.rows, (k.sx + k.xchunk - 1) / k.xchunk, 1);
-    if (prefetch) launch_hs_pf<R, true>(k, mu, dxmode, g, st);
-    else launch_hs_pf<R, false>(k, mu, dxmode, g, st);
-    return cudaGetLastError();
+    const dim3 g(k.nrowblk * k.nchunk + (k.dft_on ? 1u : 0u), 1, 1);
+    // two planes per barrier: float only (the double slots would exceed 48 KB of static shared memory)
+    if constexpr (sizeof(R) == 4) {
+        if (planes == 2) {
+            if (prefetch) return launch_hs_pf<R, true, 2>(k, mu, dxmode, g, pdl, st);
+            return launch_hs_pf<R, false, 2>(k, mu, dxmode, g, pdl, st);
+        }
+    }
+    if (prefetch) return launch_hs_pf<R, true, 1>(k, mu, dxmode, g, pdl, st);
+    return launch_hs_pf<R, false, 1>(k, mu, dxmode, g, pdl, st);
 }
 
-template cudaError_t launch_hs<float>(const HSK<float> &, bool, int, bool, cudaStream_t);
-template cudaError_t launch_hs<double>(const HSK<double> &, bool, int, bool, cudaStream_t);
+template cudaError_t launch_hs<float>(const HSK<float> &, bool, int, bool, int, bool, cudaStream_t);
+template cudaError_t launch_hs<double>(const HSK<double> &, bool, int, bool, int, bool, cudaStream_t);
 
 }  // namespace fdtd

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "yee_common.cuh"
+#include "monitors.h"
 
 namespace fdtd {
 
@@ -35,11 +36,17 @@ struct HSK {
     HSAxis<R> ax[3];
     FastDiv dsz;
     uint32_t rows, xchunk;
+    uint32_t nrowblk, nchunk;  // row blocks (ceil(sy / rows)) and x chunks (ceil(sx / xchunk))
     int32_t write_oS;
     int32_t reverse;       // 1: block row b of the grid takes the x chunk gridDim.y - 1 - b
+    int32_t dft_on;        // 1: one extra block (the last) takes the step's DFT sample of E
+    DftK<R> dft;
 };
 
+// planes: x planes per block barrier (1 or 2; float only, double takes 1); pdl: launched with
+// programmatic stream serialization
 template <typename R>
-cudaError_t launch_hs(const HSK<R> &k, bool mu, int dxmode, bool prefetch, cudaStream_t st);
+cudaError_t launch_hs(const HSK<R> &k, bool mu, int dxmode, bool prefetch, int planes, bool pdl,
+                      cudaStream_t st);
 
 }  // namespace fdtd

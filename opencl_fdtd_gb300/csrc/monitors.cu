@@ -24,17 +24,7 @@ __global__ void k_dft(const DftK<R> k)
     const int nf = k.nfreq > 0 ? k.nfreq : 1;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= k.npoint * nf) return;
-    const int p = q / nf, f = q - p * nf;
-    const double v = (double)k.field[k.index[p]];
-    if (k.nfreq > 0) {
-        const double ph = k.omega[f] * ((double)(k.step + 1) * k.dt);
-        double s, c;
-        sincos(ph, &s, &c);
-        double *a = k.accum + 2 * (int64_t)q;
-        a[0] += v * c;
-        a[1] -= v * s;
-    }
-    if (f == 0 && k.series) k.series[(int64_t)k.series_row * k.npoint + p] = v;
+    dft_sample(k, q);
 }
 
 // stage 1: block b sums cells b, b + G, b + 2G ... of the selection (G = grid size) in a

@@ -21,6 +21,27 @@ struct DftK {
     double dt;
 };
 
+// Sample q = point * nfreq + f of a DFT monitor: adds x(t) * exp(-i w t dt) in double to the
+// point's accumulator and stores x(t) in the time series (f == 0). One body for the monitor's
+// own kernel (monitors.cu) and the H+S kernel's in-launch sample (hs_fused.cu); both units are
+// compiled without FMA contraction, so the two give the same bits.
+template <typename R>
+__device__ __forceinline__ void dft_sample(const DftK<R> &k, int q)
+{
+    const int nf = k.nfreq > 0 ? k.nfreq : 1;
+    const int p = q / nf, f = q - p * nf;
+    const double v = (double)k.field[k.index[p]];
+    if (k.nfreq > 0) {
+        const double ph = k.omega[f] * ((double)(k.step + 1) * k.dt);
+        double s, c;
+        sincos(ph, &s, &c);
+        double *a = k.accum + 2 * (int64_t)q;
+        a[0] += v * c;
+        a[1] -= v * s;
+    }
+    if (f == 0 && k.series) k.series[(int64_t)k.series_row * k.npoint + p] = v;
+}
+
 template <typename R>
 struct PlaneRedK {
     const R *src;            // one component of a field

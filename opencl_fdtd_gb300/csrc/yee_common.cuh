@@ -36,6 +36,39 @@ struct FastDiv {
     }
 };
 
+// Programmatic dependent launch (fdtd_run's H+S path, FDTD_TUNE_PDL): a kernel launched with
+// programmatic stream serialization may be scheduled while the kernel before it in the stream
+// still runs; it waits here, before its first global memory access, until that kernel has
+// completed and its writes are visible, and then lets the next kernel of the stream be
+// scheduled. Without the launch attribute both instructions have no effect.
+__device__ __forceinline__ void grid_dependency_sync()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launches kern<<<g, block, 0, st>>>(arg), with programmatic stream serialization when pdl.
+template <typename K>
+inline cudaError_t launch_dependent(void (*kern)(K), dim3 g, unsigned block, cudaStream_t st,
+                                    bool pdl, const K &arg)
+{
+    if (!pdl) {
+        kern<<<g, block, 0, st>>>(arg);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = g;
+    cfg.blockDim = dim3(block, 1, 1);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, arg);
+}
+
 // CPML faces of one axis as the bulk kernels see them: the low ('n') face covers
 // c < Tn, the high ('p') face c >= s - Tp (Tp = 0 when the face never applies). Faces of one
 // axis never overlap in a bulk launch (the plan falls back to the generic kernels then), so

@@ -246,6 +246,7 @@ constexpr int EBLOCK = 256, EMINB = 3;
 template <typename R, int DX, bool BLOCH>
 __global__ void __launch_bounds__(EBLOCK, EMINB) k_bulk_e(const YeeK<R> k)
 {
+    grid_dependency_sync();
     const uint32_t j = blockIdx.x * EBLOCK + threadIdx.x;
     if (j >= k.syz) return;
     const uint32_t sx = k.sx, sy = k.sy, sz = k.sz, syz = k.syz;
@@ -641,7 +642,7 @@ static inline dim3 plane_grid(uint32_t syz, uint32_t nx)
 }
 
 template <typename R>
-cudaError_t launch_yee_e(const YeeK<R> &k, cudaStream_t st)
+cudaError_t launch_yee_e(const YeeK<R> &k, cudaStream_t st, bool pdl)
 {
     if (k.xend <= k.xbeg) return cudaSuccess;
     if (!k.bulk) {
@@ -649,16 +650,17 @@ cudaError_t launch_yee_e(const YeeK<R> &k, cudaStream_t st)
         return cudaGetLastError();
     }
     const dim3 g = bulk_grid(k.syz, k.xend - k.xbeg, k.xchunk, EBLOCK);
+    void (*kern)(YeeK<R>);
     if (k.bloch_mask) {
-        if (k.dxmode == 0) k_bulk_e<R, 0, true><<<g, EBLOCK, 0, st>>>(k);
-        else if (k.dxmode == 1) k_bulk_e<R, 1, true><<<g, EBLOCK, 0, st>>>(k);
-        else k_bulk_e<R, 2, true><<<g, EBLOCK, 0, st>>>(k);
+        if (k.dxmode == 0) kern = k_bulk_e<R, 0, true>;
+        else if (k.dxmode == 1) kern = k_bulk_e<R, 1, true>;
+        else kern = k_bulk_e<R, 2, true>;
     } else {
-        if (k.dxmode == 0) k_bulk_e<R, 0, false><<<g, EBLOCK, 0, st>>>(k);
-        else if (k.dxmode == 1) k_bulk_e<R, 1, false><<<g, EBLOCK, 0, st>>>(k);
-        else k_bulk_e<R, 2, false><<<g, EBLOCK, 0, st>>>(k);
+        if (k.dxmode == 0) kern = k_bulk_e<R, 0, false>;
+        else if (k.dxmode == 1) kern = k_bulk_e<R, 1, false>;
+        else kern = k_bulk_e<R, 2, false>;
     }
-    return cudaGetLastError();
+    return launch_dependent(kern, g, EBLOCK, st, pdl, k);
 }
 
 template <typename R, int DX, bool BLOCH>
@@ -738,7 +740,7 @@ cudaError_t launch_point_sources(const PointK<R> &k, cudaStream_t st)
 }
 
 #define FDTD_INSTANTIATE(R)                                                              \
-    template cudaError_t launch_yee_e<R>(const YeeK<R> &, cudaStream_t);               \
+    template cudaError_t launch_yee_e<R>(const YeeK<R> &, cudaStream_t, bool);         \
     template cudaError_t launch_yee_h<R>(const YeeK<R> &, bool, bool, cudaStream_t);   \
     template cudaError_t launch_poynting<R>(const SK<R> &, cudaStream_t);              \
     template cudaError_t launch_prepare<R>(const PrepK<R> &, cudaStream_t);            \

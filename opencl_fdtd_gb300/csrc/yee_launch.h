@@ -5,7 +5,8 @@
 
 namespace fdtd {
 
-template <typename R> cudaError_t launch_yee_e(const YeeK<R> &k, cudaStream_t st);
+// pdl: the bulk E kernel is launched with programmatic stream serialization (fdtd_run's H+S path)
+template <typename R> cudaError_t launch_yee_e(const YeeK<R> &k, cudaStream_t st, bool pdl = false);
 template <typename R> cudaError_t launch_yee_h(const YeeK<R> &k, bool mu, bool poynting, cudaStream_t st);
 template <typename R> cudaError_t launch_poynting(const SK<R> &k, cudaStream_t st);
 template <typename R> cudaError_t launch_prepare(const PrepK<R> &k, cudaStream_t st);

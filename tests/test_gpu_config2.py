@@ -8,6 +8,7 @@ the same inputs with the per-call loop of fdtd.py:161-179 (update_E, the soft so
 update_S). The float64 reference for the 8000-step error is the same update in float64 on the
 GPU, which equals the float64 oracle bit for bit (test_gpu_parity's float64 cases)."""
 import copy
+import math
 import os
 
 import numpy
@@ -27,12 +28,32 @@ def _wave(wl, n):
     return [wl["wave"](t) for t in range(n)]
 
 
+def _auto_hs_xchunk(sx, nrowblk, extra, nsm):
+    """The H+S kernel's automatic x chunk: among 14..24 planes the one whose grid best fills
+    whole waves of two resident blocks per SM (the smallest on a tie)."""
+    best, best_eff = 16, -1.0
+    for xc in range(14, 25):
+        waves = (nrowblk * -(-sx // xc) + extra) / (2.0 * nsm)
+        eff = waves / math.ceil(waves)
+        if eff > best_eff + 1e-12:
+            best, best_eff = xc, eff
+    return best
+
+
 def test_config2_run_path_bitwise_against_oracle():
+    """The default run path (E kernel adding the source, H+S kernel with its automatic x chunk,
+    programmatic dependent launches) at the benchmarked workload, bit for bit."""
     from opencl_fdtd_gb300 import Simulation
     wl = workloads.c2()
     g = Simulation(**copy.deepcopy(wl["kwargs"]))
     vals = _wave(wl, K)
     g.run(K, point_sources=[(wl["source_index"], vals)])
+    assert g.tuning("last_run_path") == 2 and g.tuning("pdl") == 1
+    sx, sy, sz = wl["shape"]
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    assert g.tuning("hs_xchunk_used") == _auto_hs_xchunk(sx, -(-sy // (448 // sz - 1)), 0, nsm)
+    if nsm == 152:
+        assert g.tuning("hs_xchunk_used") == 18
     c = port.PortSimulation(nthreads=os.cpu_count(), **copy.deepcopy(wl["kwargs"]))
     ind = wl["source_index"]
     for t in range(K):

@@ -215,6 +215,50 @@ def test_hs_path_equals_per_call_loop(shape, T, xchunk, nsteps):
     _same_state(a, b, True)
 
 
+@pytest.mark.parametrize("shape,T", HS_SHAPES[:4] + HS_SHAPES[6:])
+@pytest.mark.parametrize("xchunk", [1, 3, 8])
+@pytest.mark.parametrize("planes,pdl", [(2, False), (1, True), (2, True)])
+def test_hs_path_launch_options_equal_per_call_loop(shape, T, xchunk, planes, pdl):
+    """H+S path with two x planes per block barrier (odd chunks end on a one-plane group)
+    and with programmatic dependent launches of the E and H+S kernels: the per-call loop's
+    bits, with point sources added by the E kernel."""
+    rng = numpy.random.default_rng(sum(shape) + 7 * T)
+    eps = [rng.uniform(1, 4, shape).astype(numpy.float32) for _ in range(3)]
+    eps[0][1:3, 2:4, 1:4] = numpy.inf
+    init = {k: [rng.standard_normal(shape).astype(numpy.float32) for _ in range(3)] for k in "EH"}
+    pmls = [{"axis": a, "polarity": p, "thickness": T} for a in "xyz" for p in "np"
+            if 2 * T <= shape["xyz".index(a)]]
+    kw = dict(epsilon=eps, pmls=pmls, initial_fields=init, do_poynting=True)
+    N = int(numpy.prod(shape))
+    nsteps = 7
+    src = [(int(rng.integers(0, 3 * N)), [math.sin(0.3 * t) for t in range(nsteps)])]
+    a = _gpu(**copy.deepcopy(kw))
+    b = _gpu(**copy.deepcopy(kw))
+    b.tune(hs_xchunk=xchunk, hs_planes=planes, pdl=pdl)
+    assert (b.tuning("hs_planes"), b.tuning("pdl")) == (planes, int(pdl))
+    a.run(nsteps, point_sources=src, path="plain")
+    b.run(nsteps, point_sources=src, path="hs")
+    # rows longer than 224 cells take the per-update kernels
+    assert b.tuning("last_run_path") == (2 if shape[2] <= 224 else 1)
+    _same_state(a, b, True)
+
+
+@pytest.mark.parametrize("name", ["c1_small", "pml_mixed", "nonuniform", "f64_mixed"])
+def test_hs_path_launch_options_cases(name):
+    """The launch options on the golden cases (non-uniform spacing, float64, which keeps one
+    plane per barrier): the per-call loop's bits."""
+    kw, loop = cases.build(name)
+    kw["do_poynting"] = True
+    n = loop["steps"]
+    src = _sources(kw, loop, n)
+    a = _gpu(**copy.deepcopy(kw))
+    b = _gpu(**copy.deepcopy(kw))
+    b.tune(hs_planes=2, pdl=True, hs_dft=True)
+    a.run(n, point_sources=src, path="plain")
+    b.run(n, point_sources=src, path="hs")
+    _same_state(a, b, True)
+
+
 @pytest.mark.parametrize("name", ["c1_small", "pml_mixed", "periodic_pec_poynting", "nonuniform", "dx_half", "f64_mixed"])
 def test_hs_path_cases(name):
     kw, loop = cases.build(name)

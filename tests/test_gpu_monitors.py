@@ -133,10 +133,14 @@ def test_monitor_on_own_queue_grows_in_order():
     assert numpy.abs(sa).max() > 0
 
 
-def test_dft_monitor_identical_on_every_run_path():
-    """The H+S path takes each step's DFT sample inside its H+S launch (E no longer changes in
-    the step by then); the series and the accumulators equal those of the per-update path and
-    of the one-pass path bit for bit, here with the monitor grown over two runs."""
+@pytest.mark.parametrize("opts", [{"hs_dft": False, "pdl": False}, {"hs_dft": True, "pdl": False},
+                                  {"hs_dft": True, "pdl": True, "hs_planes": 2}])
+def test_dft_monitor_identical_on_every_run_path(opts):
+    """The H+S path takes each step's DFT sample in one extra block of its H+S launch (the
+    default, hs_dft), or beside that launch on a side stream (E no longer changes in the step
+    by then); the
+    series and the accumulators equal those of the per-update path and of the one-pass path
+    bit for bit, here with the monitor grown over two runs."""
     rng = numpy.random.default_rng(21)
     shape = (14, 12, 10)
     eps = [rng.uniform(1, 4, shape).astype(numpy.float32) for _ in range(3)]
@@ -150,6 +154,7 @@ def test_dft_monitor_identical_on_every_run_path():
     out = {}
     for path in ("plain", "hs", "fused"):
         g = _gpu(**copy.deepcopy(kw))
+        g.tune(**opts)
         mon = g.dft_monitor(pts, om)
         g.run(n, point_sources=[(src[0][0], src[0][1][:n])], monitor=mon, path=path)
         g.run(n, point_sources=[(src[0][0], src[0][1][n:])], monitor=mon, path=path)
