@@ -473,8 +473,9 @@ int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
         if ((rc = timer.mark(t, 1))) return rc;
         if ((rc = lbc_after_e(p, b, H[a], st))) return rc;
         if (!added && src && src->n > 0 && (rc = run_point_sources<R>(p, &bb, st, src, t))) return rc;
-        // the H+S launch leaves E unchanged: the step's DFT sample runs on the side stream beside
-        // it, and the next step's E update waits for it (below)
+        // the H+S launch leaves E unchanged, so the step's DFT sample of E is taken by its last
+        // block, or (hs_dft off) runs on the side stream beside it and the next step's E update
+        // waits for it (above)
         k.dft_on = dft_in ? 1 : 0;
         if (dft_in) k.dft = dft_args<R>(p, b->E, mon, t);
         if (dft_side) {

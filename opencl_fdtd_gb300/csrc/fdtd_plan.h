@@ -30,8 +30,8 @@ struct FdtdPlan {
     int32_t pdl;                // H+S path: programmatic dependent launches of E and H+S
     int32_t timing;             // fdtd_run's H+S path records per-kernel CUDA events
     int32_t *status = nullptr;  // device word: bits of bounded waits inside kernels that ran out
-    // side stream of fdtd_run's H+S path: the step's DFT monitor sample runs there, beside the
-    // H+S launch (which leaves E unchanged); created on first use
+    // side stream of fdtd_run's H+S path when hs_dft is off: the step's DFT monitor sample runs
+    // there, beside the H+S launch (which leaves E unchanged); created on first use
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double kernel_ms[2];        // last timed run: mean update_E and H+S launch times (ms)
