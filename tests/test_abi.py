@@ -34,6 +34,21 @@ def test_library_loads_and_exports_every_declared_symbol():
     assert lib.fdtd_abi_version() == 1
 
 
+def test_header_constants_match_the_python_mirror():
+    """Every integer #define of the header (status codes, dtypes, tuning and read-back keys,
+    run paths, storage and precision codes) has the same value in the ctypes mirror."""
+    defs = {}
+    for h in HEADERS:
+        defs.update(re.findall(r"^#define\s+(FDTD_\w+)\s+(-?\d+)\s*(?:/\*.*)?$", open(h).read(), flags=re.M))
+    assert len(defs) >= 40
+    lib = _lib.load()
+    for name, value in defs.items():
+        if name == "FDTD_ABI_VERSION":
+            assert lib.fdtd_abi_version() == int(value)
+            continue
+        assert getattr(_lib, name) == int(value), name
+
+
 def test_errors_without_a_gpu_call():
     lib = _lib.load()
     plan = ctypes.c_void_p()
