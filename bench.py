@@ -599,7 +599,8 @@ def main():
     step_gbs = step_bytes / (hp["ms_per_step"] * 1e-3) / 1e9
     # launch options of the H+S path as the timed run used them
     launch = ({"hs_xchunk": sim.tuning("hs_xchunk_used"), "pdl": sim.tuning("pdl"),
-               "dft_in_hs_launch": sim.tuning("hs_dft"), "e_xchunk": sim.tuning("xchunk")}
+               "dft_in_hs_launch": sim.tuning("hs_dft"), "e_xchunk": sim.tuning("xchunk"),
+               "e_form": sim.tuning("e_form")}
               if head == "hs" else None)
 
     e2e = None

@@ -150,6 +150,9 @@ int fdtd_plan_destroy(FdtdPlan *plan);
  *                 programmatic stream serialization (each may be scheduled while the kernel
  *                 before it finishes, and waits for it before touching memory); 0: plain stream
  *                 order
+ *   E_FORM        form of the bulk E kernel: 0 loads the next x plane one iteration ahead at
+ *                 three blocks of 256 threads per SM; 1 (default) / 2 load each plane when it is
+ *                 updated, at four / five blocks per SM (all forms give the same results)
  *   TIMING        1: fdtd_run records CUDA events around its kernels on up to 64 steps spread
  *                 over the call (update_E and H+S on the H+S path, the step kernel on the
  *                 one-pass path) and waits for the stream before it returns (profiling; read
@@ -168,6 +171,7 @@ int fdtd_plan_destroy(FdtdPlan *plan);
 #define FDTD_TUNE_HS_PLANES 12
 #define FDTD_TUNE_HS_DFT 13
 #define FDTD_TUNE_PDL 14
+#define FDTD_TUNE_E_FORM 15
 /* Read-only keys of fdtd_plan_get: the path of the last fdtd_run (FDTD_PATH_*), the tiling
  * of its last one-pass launch (own rows per tile, x chunk, stages, threads per block, shape)
  * and the x chunk of its last H+S launch. */

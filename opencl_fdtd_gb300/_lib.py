@@ -37,6 +37,7 @@ FDTD_TUNE_HS_REVERSE = 11
 FDTD_TUNE_HS_PLANES = 12
 FDTD_TUNE_HS_DFT = 13
 FDTD_TUNE_PDL = 14
+FDTD_TUNE_E_FORM = 15
 FDTD_GET_LAST_RUN_PATH = 100
 FDTD_GET_STEP_ROWS = 101
 FDTD_GET_STEP_XCHUNK = 102

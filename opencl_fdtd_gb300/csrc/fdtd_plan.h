@@ -13,6 +13,7 @@ struct FdtdPlan {
     size_t elem;                // bytes per element of the plan's dtype
     int device;                 // device that was current at creation
     int32_t xchunk;             // x planes a bulk-kernel thread marches
+    int32_t eform;              // form of the bulk E kernel (FDTD_TUNE_E_FORM)
     uint32_t slab;              // x planes per L2-resident slab in fdtd_run (0: whole grid)
     uint32_t fused_rows;        // own rows of a one-pass step tile (0: the most that fit)
     uint32_t fused_xchunk;      // x planes one block of the one-pass step marches (0: automatic)

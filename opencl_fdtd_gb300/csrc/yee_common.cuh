@@ -109,7 +109,8 @@ struct YeeK {
     uint64_t N;
     R dt, inv_d;
     const R *inv_tab[3];
-    int32_t nface, bloch_mask, dxmode, _pad;
+    int32_t nface, bloch_mask, dxmode;
+    int32_t eform;              // form of the bulk E kernel (0 prefetch, 1 / 2 per-plane loads)
     R br[3], bi[3];
     FaceK<R> face[6];
     AxisK<R> ax[3];

@@ -623,7 +623,7 @@ class Simulation:
              fused_xchunk: int = None, hs_xchunk: int = None, hs_prefetch: bool = None,
              fused_stages: int = None, fused_tma: bool = None, fused_shape: int = None,
              hs_reverse: bool = None, hs_planes: int = None, hs_dft: bool = None,
-             pdl: bool = None):
+             pdl: bool = None, e_form: int = None):
         """Kernel tiling and launch options (None keeps a value); results do not depend on them.
 
         fused_rows / fused_xchunk / fused_stages: own y rows of a one-pass step tile, x planes
@@ -633,7 +633,9 @@ class Simulation:
         the 'hs' path takes its x chunks in descending order (default) or ascending;
         hs_planes: x planes per block barrier of the H+S kernel (1 or 2); hs_dft: the step's
         DFT monitor sample is taken inside the H+S launch instead of on a side stream; pdl:
-        the E and H+S kernels of the 'hs' path use programmatic dependent launch."""
+        the E and H+S kernels of the 'hs' path use programmatic dependent launch; e_form: form
+        of the bulk E kernel (0 next plane loaded ahead, 1 (default) / 2 per-plane loads at
+        four / five blocks per SM)."""
         for key, val in ((_lib.FDTD_TUNE_XCHUNK, xchunk), (_lib.FDTD_TUNE_SLAB, slab),
                          (_lib.FDTD_TUNE_FUSED_ROWS, fused_rows),
                          (_lib.FDTD_TUNE_FUSED_XCHUNK, fused_xchunk),
@@ -645,7 +647,8 @@ class Simulation:
                          (_lib.FDTD_TUNE_HS_REVERSE, None if hs_reverse is None else int(hs_reverse)),
                          (_lib.FDTD_TUNE_HS_PLANES, hs_planes),
                          (_lib.FDTD_TUNE_HS_DFT, None if hs_dft is None else int(hs_dft)),
-                         (_lib.FDTD_TUNE_PDL, None if pdl is None else int(pdl))):
+                         (_lib.FDTD_TUNE_PDL, None if pdl is None else int(pdl)),
+                         (_lib.FDTD_TUNE_E_FORM, e_form)):
             if val is not None:
                 _lib.check(self._lib.fdtd_plan_tune(self._plan, key, int(val)))
 

@@ -259,6 +259,38 @@ def test_hs_path_launch_options_cases(name):
     _same_state(a, b, True)
 
 
+@pytest.mark.parametrize("form", [0, 2])
+@pytest.mark.parametrize("name", cases.CASE_NAMES)
+def test_e_kernel_forms_equal_default(name, form):
+    """The bulk E kernel's other forms (0: next plane loaded ahead at three blocks per SM; 2:
+    per-plane loads at five) against the default (per-plane loads at four blocks per SM):
+    every golden case (Bloch F/G, non-uniform spacing, float64, overlapping faces) through the
+    per-call loop, and the run path, bit for bit."""
+    from opencl_fdtd_gb300 import Simulation
+
+    def tuned(**kw):
+        s = Simulation(**kw)
+        s.tune(e_form=form)
+        assert s.tuning("e_form") == form
+        return s
+
+    a = cases.run_case(Simulation, name)
+    b = cases.run_case(tuned, name)
+    oa, ob = cases.outputs(a, name), cases.outputs(b, name)
+    for k in oa:
+        assert numpy.array_equal(oa[k], ob[k]), (name, k)
+    kw, loop = cases.build(name)
+    if not kw.get("bloch_boundaries"):
+        kw["do_poynting"] = True
+        n = loop["steps"]
+        src = _sources(kw, loop, n)
+        c = _gpu(**copy.deepcopy(kw))
+        d = tuned(**copy.deepcopy(kw))
+        c.run(n, point_sources=src)
+        d.run(n, point_sources=src)
+        _same_state(c, d, True)
+
+
 @pytest.mark.parametrize("name", ["c1_small", "pml_mixed", "periodic_pec_poynting", "nonuniform", "dx_half", "f64_mixed"])
 def test_hs_path_cases(name):
     kw, loop = cases.build(name)
