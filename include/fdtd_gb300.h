@@ -142,8 +142,6 @@ int fdtd_plan_destroy(FdtdPlan *plan);
  *                 (two blocks per SM, the default)
  *   HS_REVERSE    1 (default): the H+S kernel takes its x chunks in descending order, so that it
  *                 starts on the planes update_E wrote last (still in L2); 0: ascending
- *   HS_PLANES     x planes the H+S kernel evaluates per block barrier: 1 (default) or 2 (float
- *                 only; double takes 1)
  *   HS_DFT        1 (default): on the H+S path the step's DFT monitor sample is taken by one extra
  *                 block of the H+S launch; 0: by the monitor kernel on a side stream beside it
  *   PDL           1 (default): on the H+S path the E and H+S kernels are launched with
@@ -151,8 +149,8 @@ int fdtd_plan_destroy(FdtdPlan *plan);
  *                 before it finishes, and waits for it before touching memory); 0: plain stream
  *                 order
  *   E_FORM        form of the bulk E kernel: 0 loads the next x plane one iteration ahead at
- *                 three blocks of 256 threads per SM; 1 (default) / 2 load each plane when it is
- *                 updated, at four / five blocks per SM (all forms give the same results)
+ *                 three blocks of 256 threads per SM; 1 (default) loads each plane when it is
+ *                 updated, at four blocks per SM (both give the same results)
  *   TIMING        1: fdtd_run records CUDA events around its kernels on up to 64 steps spread
  *                 over the call (update_E and H+S on the H+S path, the step kernel on the
  *                 one-pass path) and waits for the stream before it returns (profiling; read
@@ -168,7 +166,6 @@ int fdtd_plan_destroy(FdtdPlan *plan);
 #define FDTD_TUNE_FUSED_TMA 9
 #define FDTD_TUNE_FUSED_SHAPE 10
 #define FDTD_TUNE_HS_REVERSE 11
-#define FDTD_TUNE_HS_PLANES 12
 #define FDTD_TUNE_HS_DFT 13
 #define FDTD_TUNE_PDL 14
 #define FDTD_TUNE_E_FORM 15

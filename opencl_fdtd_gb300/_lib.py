@@ -34,7 +34,6 @@ FDTD_TUNE_FUSED_STAGES = 8
 FDTD_TUNE_FUSED_TMA = 9
 FDTD_TUNE_FUSED_SHAPE = 10
 FDTD_TUNE_HS_REVERSE = 11
-FDTD_TUNE_HS_PLANES = 12
 FDTD_TUNE_HS_DFT = 13
 FDTD_TUNE_PDL = 14
 FDTD_TUNE_E_FORM = 15

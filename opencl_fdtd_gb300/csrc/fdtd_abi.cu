@@ -501,7 +501,7 @@ int run_hs(FdtdPlan *p, const FdtdBuffers *b, cudaStream_t st, int nsteps,
             }
         k.write_oS = t == nsteps - 1;
         if ((rc = timer.mark(t, 2))) return rc;
-        if ((rc = check_cuda(launch_hs<R>(k, p->d.has_mu != 0, dxmode, p->hs_prefetch != 0, p->hs_planes, pdl, st), "H+S launch"))) return rc;
+        if ((rc = check_cuda(launch_hs<R>(k, p->d.has_mu != 0, dxmode, p->hs_prefetch != 0, pdl, st), "H+S launch"))) return rc;
         if ((rc = timer.mark(t, 3))) return rc;
         if ((rc = lbc_after_h(p, b, H[o], st))) return rc;
     }
@@ -938,7 +938,6 @@ int fdtd_plan_create(const FdtdDesc *desc, FdtdPlan **out)
     p->hs_xchunk = 0;
     p->hs_prefetch = 0;
     p->hs_reverse = 1;
-    p->hs_planes = 1;
     // per-plane loads at four blocks per SM: update_E 0.110 -> 0.105 ms on the 395x345x73 grid
     p->eform = 1;
     p->hs_xchunk_used = 0;
@@ -1054,10 +1053,6 @@ int fdtd_plan_tune(FdtdPlan *p, int32_t key, int32_t value)
         if (value != 0 && value != 1) return fail(FDTD_ERR_INVALID, "hs_prefetch must be 0 or 1");
         p->hs_prefetch = value;
         return FDTD_OK;
-    case FDTD_TUNE_HS_PLANES:
-        if (value != 1 && value != 2) return fail(FDTD_ERR_INVALID, "hs_planes must be 1 or 2");
-        p->hs_planes = value;
-        return FDTD_OK;
     case FDTD_TUNE_HS_DFT:
         if (value != 0 && value != 1) return fail(FDTD_ERR_INVALID, "hs_dft must be 0 or 1");
         p->hs_dft = value;
@@ -1067,7 +1062,7 @@ int fdtd_plan_tune(FdtdPlan *p, int32_t key, int32_t value)
         p->pdl = value;
         return FDTD_OK;
     case FDTD_TUNE_E_FORM:
-        if (value < 0 || value > 2) return fail(FDTD_ERR_INVALID, "e_form must be 0, 1 or 2");
+        if (value != 0 && value != 1) return fail(FDTD_ERR_INVALID, "e_form must be 0 or 1");
         p->eform = value;
         return FDTD_OK;
     default:
@@ -1095,7 +1090,6 @@ int fdtd_plan_get(const FdtdPlan *p, int32_t key, int32_t *value)
     case FDTD_GET_STEP_THREADS: *value = p->step_cfg[3]; return FDTD_OK;
     case FDTD_TUNE_HS_XCHUNK: *value = (int32_t)p->hs_xchunk; return FDTD_OK;
     case FDTD_TUNE_HS_PREFETCH: *value = p->hs_prefetch; return FDTD_OK;
-    case FDTD_TUNE_HS_PLANES: *value = p->hs_planes; return FDTD_OK;
     case FDTD_GET_HS_XCHUNK_USED: *value = p->hs_xchunk_used; return FDTD_OK;
     case FDTD_TUNE_HS_DFT: *value = p->hs_dft; return FDTD_OK;
     case FDTD_TUNE_PDL: *value = p->pdl; return FDTD_OK;

@@ -25,7 +25,6 @@ struct FdtdPlan {
     uint32_t hs_xchunk;         // x planes one block of the H+S kernel marches
     int32_t hs_prefetch;        // H+S kernel issues the next plane's loads early
     int32_t hs_reverse;         // H+S kernel takes its x chunks in descending order
-    int32_t hs_planes;          // x planes per block barrier of the H+S kernel (1 or 2)
     int32_t hs_xchunk_used;     // x chunk of the last H+S launch (hs_xchunk or the automatic one)
     int32_t hs_dft;             // H+S path: the DFT sample in the H+S launch, not a side stream
     int32_t pdl;                // H+S path: programmatic dependent launches of E and H+S

@@ -215,9 +215,8 @@ __device__ __forceinline__ void hs_s(const HSK<R> &k, const R *q, uint32_t t, ui
 // Thread t of a block works on window row w = t / sz (cell z = t % sz): row 0 is the halo row
 // y0 - 1 (wrapped), whose products only feed S of row y0; rows 1..rows are the block's own
 // rows y0 .. y0 + rows - 1. Every thread evaluates exactly one cell per plane, so a barrier
-// waits for no extra work. The products of PB consecutive planes go to shared memory slots,
-// then one barrier, then S of those planes; the slot groups alternate, which is what lets one
-// barrier per PB planes suffice.
+// waits for no extra work. The products go to shared memory slots that alternate by plane,
+// which is what lets one barrier per plane suffice.
 // PF: issue the next plane's loads before the current plane's arithmetic (one block per SM
 // with room for both sets of registers); otherwise (two blocks per SM) they are issued after
 // the products are stored, so that the last plane's are in flight during the barrier and the
@@ -226,10 +225,10 @@ __device__ __forceinline__ void hs_s(const HSK<R> &k, const R *q, uint32_t t, ui
 // blocks fastest). With dft_on one more block (the last) takes the step's DFT monitor sample
 // of E, which this launch leaves unchanged; a single block keeps a grid that fills whole
 // waves of resident blocks doing so.
-template <typename R, int DX, bool MU, bool PF, int PB>
+template <typename R, int DX, bool MU, bool PF>
 __global__ void __launch_bounds__(HS_THREADS, PF ? 1 : 2) k_bulk_hs(const HSK<R> k)
 {
-    __shared__ R sS[2 * PB][6][HS_THREADS];
+    __shared__ R sS[2][6][HS_THREADS];
     grid_dependency_sync();
     const uint32_t t = threadIdx.x;
     const uint32_t chunk = blockIdx.x / k.nrowblk;
@@ -280,101 +279,54 @@ __global__ void __launch_bounds__(HS_THREADS, PF ? 1 : 2) k_bulk_hs(const HSK<R>
     HSLoad<R> cur;
     uint32_t i = xa * syz + j;
     if (act) hs_load<R, MU>(k, xa, i, dpy, dpz, hs_face<R>(k.ax[0], sx, xa), fy, fz, y, z, cur);
-    if constexpr (PB == 1) {
-        for (uint32_t x = xa; x < xb; ++x, i += syz) {
-            const HSF fx = hs_face<R>(k.ax[0], sx, x);
-            const int slot = (int)(x & 1u);
-            HSLoad<R> nxt;
-            if (act) {
-                if (PF && x + 1u < xb) hs_load<R, MU>(k, x + 1u, i + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, nxt);
-                R os[6];
-                hs_math<R, DX, MU>(k, x, y, z, i, fx, fy, fz, cur, own, os, cy, cz);
+    for (uint32_t x = xa; x < xb; ++x, i += syz) {
+        const HSF fx = hs_face<R>(k.ax[0], sx, x);
+        const int slot = (int)(x & 1u);
+        HSLoad<R> nxt;
+        if (act) {
+            if (PF && x + 1u < xb) hs_load<R, MU>(k, x + 1u, i + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, nxt);
+            R os[6];
+            hs_math<R, DX, MU>(k, x, y, z, i, fx, fy, fz, cur, own, os, cy, cz);
 #pragma unroll
-                for (int c = 0; c < 6; ++c) sS[slot][c][t] = os[c];
-                if (own && k.write_oS) {
+            for (int c = 0; c < 6; ++c) sS[slot][c][t] = os[c];
+            if (own && k.write_oS) {
 #pragma unroll
-                    for (int c = 0; c < 6; ++c) k.oS[(uint64_t)c * N + i] = os[c];
-                }
-                // the next plane's loads fly during the barrier and the S assembly
-                if (!PF && x + 1u < xb)
-                    hs_load<R, MU>(k, x + 1u, i + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, cur);
+                for (int c = 0; c < 6; ++c) k.oS[(uint64_t)c * N + i] = os[c];
             }
-            __syncthreads();
-            if (own) hs_s<R>(k, sS[slot][0], t, z, i, prev_yx, prev_zx);
-            if (PF && act) cur = nxt;
+            // the next plane's loads fly during the barrier and the S assembly
+            if (!PF && x + 1u < xb)
+                hs_load<R, MU>(k, x + 1u, i + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, cur);
         }
-    } else {
-        for (uint32_t xg = xa; xg < xb; xg += PB, i += PB * syz) {
-            // slot group: xg / PB advances by one per group, so the groups alternate
-            const int base = (int)((xg / (uint32_t)PB) & 1u) * PB;
-#pragma unroll
-            for (int p = 0; p < PB; ++p) {
-                const uint32_t x = xg + (uint32_t)p;
-                if (x >= xb) break;   // block-uniform
-                const uint32_t ix = i + (uint32_t)p * syz;
-                if (act) {
-                    const HSF fx = hs_face<R>(k.ax[0], sx, x);
-                    HSLoad<R> nxt;
-                    if (PF && x + 1u < xb) hs_load<R, MU>(k, x + 1u, ix + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, nxt);
-                    R os[6];
-                    hs_math<R, DX, MU>(k, x, y, z, ix, fx, fy, fz, cur, own, os, cy, cz);
-#pragma unroll
-                    for (int c = 0; c < 6; ++c) sS[base + p][c][t] = os[c];
-                    if (own && k.write_oS) {
-#pragma unroll
-                        for (int c = 0; c < 6; ++c) k.oS[(uint64_t)c * N + ix] = os[c];
-                    }
-                    // the next plane's loads (those of the group's last plane fly during the
-                    // barrier and the S assembly)
-                    if (!PF && x + 1u < xb)
-                        hs_load<R, MU>(k, x + 1u, ix + syz, dpy, dpz, hs_face<R>(k.ax[0], sx, x + 1u), fy, fz, y, z, cur);
-                    if (PF) cur = nxt;
-                }
-            }
-            __syncthreads();
-            if (own) {
-#pragma unroll
-                for (int p = 0; p < PB; ++p) {
-                    if (xg + (uint32_t)p >= xb) break;
-                    hs_s<R>(k, sS[base + p][0], t, z, i + (uint32_t)p * syz, prev_yx, prev_zx);
-                }
-            }
-        }
+        __syncthreads();
+        if (own) hs_s<R>(k, sS[slot][0], t, z, i, prev_yx, prev_zx);
+        if (PF && act) cur = nxt;
     }
 }
 
-template <typename R, int DX, bool PF, int PB>
+template <typename R, int DX, bool PF>
 static cudaError_t launch_hs_dx(const HSK<R> &k, bool mu, dim3 g, bool pdl, cudaStream_t st)
 {
-    if (mu) return launch_dependent(k_bulk_hs<R, DX, true, PF, PB>, g, HS_THREADS, st, pdl, k);
-    return launch_dependent(k_bulk_hs<R, DX, false, PF, PB>, g, HS_THREADS, st, pdl, k);
+    if (mu) return launch_dependent(k_bulk_hs<R, DX, true, PF>, g, HS_THREADS, st, pdl, k);
+    return launch_dependent(k_bulk_hs<R, DX, false, PF>, g, HS_THREADS, st, pdl, k);
 }
 
-template <typename R, bool PF, int PB>
+template <typename R, bool PF>
 static cudaError_t launch_hs_pf(const HSK<R> &k, bool mu, int dxmode, dim3 g, bool pdl, cudaStream_t st)
 {
-    if (dxmode == 0) return launch_hs_dx<R, 0, PF, PB>(k, mu, g, pdl, st);
-    if (dxmode == 1) return launch_hs_dx<R, 1, PF, PB>(k, mu, g, pdl, st);
-    return launch_hs_dx<R, 2, PF, PB>(k, mu, g, pdl, st);
+    if (dxmode == 0) return launch_hs_dx<R, 0, PF>(k, mu, g, pdl, st);
+    if (dxmode == 1) return launch_hs_dx<R, 1, PF>(k, mu, g, pdl, st);
+    return launch_hs_dx<R, 2, PF>(k, mu, g, pdl, st);
 }
 
 template <typename R>
-cudaError_t launch_hs(const HSK<R> &k, bool mu, int dxmode, bool prefetch, int planes, bool pdl,
-                      cudaStream_t st)
+cudaError_t launch_hs(const HSK<R> &k, bool mu, int dxmode, bool prefetch, bool pdl, cudaStream_t st)
 {
     const dim3 g(k.nrowblk * k.nchunk + (k.dft_on ? 1u : 0u), 1, 1);
-    // two planes per barrier: float only (the double slots would exceed 48 KB of static shared memory)
-    if constexpr (sizeof(R) == 4) {
-        if (planes == 2) {
-            if (prefetch) return launch_hs_pf<R, true, 2>(k, mu, dxmode, g, pdl, st);
-            return launch_hs_pf<R, false, 2>(k, mu, dxmode, g, pdl, st);
-        }
-    }
-    if (prefetch) return launch_hs_pf<R, true, 1>(k, mu, dxmode, g, pdl, st);
-    return launch_hs_pf<R, false, 1>(k, mu, dxmode, g, pdl, st);
+    if (prefetch) return launch_hs_pf<R, true>(k, mu, dxmode, g, pdl, st);
+    return launch_hs_pf<R, false>(k, mu, dxmode, g, pdl, st);
 }
 
-template cudaError_t launch_hs<float>(const HSK<float> &, bool, int, bool, int, bool, cudaStream_t);
-template cudaError_t launch_hs<double>(const HSK<double> &, bool, int, bool, int, bool, cudaStream_t);
+template cudaError_t launch_hs<float>(const HSK<float> &, bool, int, bool, bool, cudaStream_t);
+template cudaError_t launch_hs<double>(const HSK<double> &, bool, int, bool, bool, cudaStream_t);
 
 }  // namespace fdtd

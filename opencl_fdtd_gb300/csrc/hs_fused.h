@@ -43,10 +43,8 @@ struct HSK {
     DftK<R> dft;
 };
 
-// planes: x planes per block barrier (1 or 2; float only, double takes 1); pdl: launched with
-// programmatic stream serialization
+// pdl: launched with programmatic stream serialization
 template <typename R>
-cudaError_t launch_hs(const HSK<R> &k, bool mu, int dxmode, bool prefetch, int planes, bool pdl,
-                      cudaStream_t st);
+cudaError_t launch_hs(const HSK<R> &k, bool mu, int dxmode, bool prefetch, bool pdl, cudaStream_t st);
 
 }  // namespace fdtd

@@ -110,7 +110,7 @@ struct YeeK {
     R dt, inv_d;
     const R *inv_tab[3];
     int32_t nface, bloch_mask, dxmode;
-    int32_t eform;              // form of the bulk E kernel (0 prefetch, 1 / 2 per-plane loads)
+    int32_t eform;              // form of the bulk E kernel (0 next plane ahead, 1 per-plane loads)
     R br[3], bi[3];
     FaceK<R> face[6];
     AxisK<R> ax[3];

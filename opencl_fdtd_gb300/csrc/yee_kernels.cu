@@ -244,13 +244,13 @@ struct ELoad {
 constexpr int EBLOCK = 256, EMINB = 3;
 
 // Forms of the bulk E kernel (FDTD_TUNE_E_FORM): 0 loads the next plane one iteration ahead
-// (80 registers, three blocks per SM); 1 (the default) and 2 load each plane when it is
-// updated, at four (64 registers) and five (48 registers, spilling) blocks per SM. Same
-// arithmetic in every form. On the 395x345x73 grid: 0.110, 0.105 and 0.131 ms.
+// (80 registers, three blocks per SM); 1 (the default) loads each plane when it is updated, at
+// four blocks per SM (64 registers). Same arithmetic in both. On the 395x345x73 grid: 0.110
+// and 0.105 ms (a per-plane form at five blocks per SM spilled 80 B and took 0.131 ms).
 template <int FORM>
 struct EForm {
     static constexpr bool prefetch = FORM == 0;
-    static constexpr int min_blocks = FORM == 0 ? EMINB : FORM == 1 ? 4 : 5;
+    static constexpr int min_blocks = FORM == 0 ? EMINB : 4;
 };
 
 template <typename R, int DX, bool BLOCH, int FORM>
@@ -661,7 +661,6 @@ template <typename R, bool BLOCH, int DX>
 static void (*bulk_e_form(int form))(YeeK<R>)
 {
     if (form == 1) return k_bulk_e<R, DX, BLOCH, 1>;
-    if (form == 2) return k_bulk_e<R, DX, BLOCH, 2>;
     return k_bulk_e<R, DX, BLOCH, 0>;
 }
 

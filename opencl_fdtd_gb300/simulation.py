@@ -622,20 +622,19 @@ class Simulation:
     def tune(self, xchunk: int = None, slab: int = None, fused_rows: int = None,
              fused_xchunk: int = None, hs_xchunk: int = None, hs_prefetch: bool = None,
              fused_stages: int = None, fused_tma: bool = None, fused_shape: int = None,
-             hs_reverse: bool = None, hs_planes: int = None, hs_dft: bool = None,
-             pdl: bool = None, e_form: int = None):
+             hs_reverse: bool = None, hs_dft: bool = None, pdl: bool = None,
+             e_form: int = None):
         """Kernel tiling and launch options (None keeps a value); results do not depend on them.
 
         fused_rows / fused_xchunk / fused_stages: own y rows of a one-pass step tile, x planes
         of a block, planes in its shared-memory ring (0: automatic); fused_tma: stage the rows
         of non-wrapping tiles with bulk asynchronous copies (default) or per element;
         fused_shape: block shape (1 large, 2 small, 0 automatic); hs_reverse: the H+S kernel of
-        the 'hs' path takes its x chunks in descending order (default) or ascending;
-        hs_planes: x planes per block barrier of the H+S kernel (1 or 2); hs_dft: the step's
-        DFT monitor sample is taken inside the H+S launch instead of on a side stream; pdl:
-        the E and H+S kernels of the 'hs' path use programmatic dependent launch; e_form: form
-        of the bulk E kernel (0 next plane loaded ahead, 1 (default) / 2 per-plane loads at
-        four / five blocks per SM)."""
+        the 'hs' path takes its x chunks in descending order (default) or ascending; hs_dft:
+        the step's DFT monitor sample is taken inside the H+S launch (default) instead of on a
+        side stream; pdl: the E and H+S kernels of the 'hs' path use programmatic dependent
+        launch (default); e_form: form of the bulk E kernel (0 next plane loaded ahead at three
+        blocks per SM, 1 (default) per-plane loads at four)."""
         for key, val in ((_lib.FDTD_TUNE_XCHUNK, xchunk), (_lib.FDTD_TUNE_SLAB, slab),
                          (_lib.FDTD_TUNE_FUSED_ROWS, fused_rows),
                          (_lib.FDTD_TUNE_FUSED_XCHUNK, fused_xchunk),
@@ -645,7 +644,6 @@ class Simulation:
                          (_lib.FDTD_TUNE_FUSED_TMA, None if fused_tma is None else int(fused_tma)),
                          (_lib.FDTD_TUNE_FUSED_SHAPE, fused_shape),
                          (_lib.FDTD_TUNE_HS_REVERSE, None if hs_reverse is None else int(hs_reverse)),
-                         (_lib.FDTD_TUNE_HS_PLANES, hs_planes),
                          (_lib.FDTD_TUNE_HS_DFT, None if hs_dft is None else int(hs_dft)),
                          (_lib.FDTD_TUNE_PDL, None if pdl is None else int(pdl)),
                          (_lib.FDTD_TUNE_E_FORM, e_form)):

@@ -216,12 +216,12 @@ def test_hs_path_equals_per_call_loop(shape, T, xchunk, nsteps):
 
 
 @pytest.mark.parametrize("shape,T", HS_SHAPES[:4] + HS_SHAPES[6:])
-@pytest.mark.parametrize("xchunk", [1, 3, 8])
-@pytest.mark.parametrize("planes,pdl", [(2, False), (1, True), (2, True)])
-def test_hs_path_launch_options_equal_per_call_loop(shape, T, xchunk, planes, pdl):
-    """H+S path with two x planes per block barrier (odd chunks end on a one-plane group)
-    and with programmatic dependent launches of the E and H+S kernels: the per-call loop's
-    bits, with point sources added by the E kernel."""
+@pytest.mark.parametrize("xchunk", [0, 1, 3, 8])
+@pytest.mark.parametrize("pdl", [False, True])
+def test_hs_path_launch_options_equal_per_call_loop(shape, T, xchunk, pdl):
+    """H+S path with and without programmatic dependent launches of the E and H+S kernels,
+    at the automatic (0) and at fixed x chunks: the per-call loop's bits, with point sources
+    added by the E kernel."""
     rng = numpy.random.default_rng(sum(shape) + 7 * T)
     eps = [rng.uniform(1, 4, shape).astype(numpy.float32) for _ in range(3)]
     eps[0][1:3, 2:4, 1:4] = numpy.inf
@@ -234,8 +234,8 @@ def test_hs_path_launch_options_equal_per_call_loop(shape, T, xchunk, planes, pd
     src = [(int(rng.integers(0, 3 * N)), [math.sin(0.3 * t) for t in range(nsteps)])]
     a = _gpu(**copy.deepcopy(kw))
     b = _gpu(**copy.deepcopy(kw))
-    b.tune(hs_xchunk=xchunk, hs_planes=planes, pdl=pdl)
-    assert (b.tuning("hs_planes"), b.tuning("pdl")) == (planes, int(pdl))
+    b.tune(hs_xchunk=xchunk, pdl=pdl)
+    assert (b.tuning("hs_xchunk"), b.tuning("pdl")) == (xchunk, int(pdl))
     a.run(nsteps, point_sources=src, path="plain")
     b.run(nsteps, point_sources=src, path="hs")
     # rows longer than 224 cells take the per-update kernels
@@ -245,27 +245,27 @@ def test_hs_path_launch_options_equal_per_call_loop(shape, T, xchunk, planes, pd
 
 @pytest.mark.parametrize("name", ["c1_small", "pml_mixed", "nonuniform", "f64_mixed"])
 def test_hs_path_launch_options_cases(name):
-    """The launch options on the golden cases (non-uniform spacing, float64, which keeps one
-    plane per barrier): the per-call loop's bits."""
+    """The default launch options (programmatic dependent launch, DFT sample in the H+S
+    launch) on golden cases with non-uniform spacing and float64: the per-call loop's bits."""
     kw, loop = cases.build(name)
     kw["do_poynting"] = True
     n = loop["steps"]
     src = _sources(kw, loop, n)
     a = _gpu(**copy.deepcopy(kw))
     b = _gpu(**copy.deepcopy(kw))
-    b.tune(hs_planes=2, pdl=True, hs_dft=True)
+    b.tune(pdl=True, hs_dft=True)
     a.run(n, point_sources=src, path="plain")
     b.run(n, point_sources=src, path="hs")
     _same_state(a, b, True)
 
 
-@pytest.mark.parametrize("form", [0, 2])
+@pytest.mark.parametrize("form", [0])
 @pytest.mark.parametrize("name", cases.CASE_NAMES)
 def test_e_kernel_forms_equal_default(name, form):
-    """The bulk E kernel's other forms (0: next plane loaded ahead at three blocks per SM; 2:
-    per-plane loads at five) against the default (per-plane loads at four blocks per SM):
-    every golden case (Bloch F/G, non-uniform spacing, float64, overlapping faces) through the
-    per-call loop, and the run path, bit for bit."""
+    """The bulk E kernel's other form (0: next plane loaded ahead at three blocks per SM)
+    against the default (per-plane loads at four blocks per SM): every golden case (Bloch F/G,
+    non-uniform spacing, float64, overlapping faces) through the per-call loop, and the run
+    path, bit for bit."""
     from opencl_fdtd_gb300 import Simulation
 
     def tuned(**kw):

@@ -134,7 +134,7 @@ def test_monitor_on_own_queue_grows_in_order():
 
 
 @pytest.mark.parametrize("opts", [{"hs_dft": False, "pdl": False}, {"hs_dft": True, "pdl": False},
-                                  {"hs_dft": True, "pdl": True, "hs_planes": 2}])
+                                  {"hs_dft": True, "pdl": True}])
 def test_dft_monitor_identical_on_every_run_path(opts):
     """The H+S path takes each step's DFT sample in one extra block of its H+S launch (the
     default, hs_dft), or beside that launch on a side stream (E no longer changes in the step
